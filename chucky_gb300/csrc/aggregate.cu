@@ -1,0 +1,180 @@
+// (d) Shard aggregation: compressed chunks -> shard-ordered byte runs.
+//
+// Per level of a batch (src/gpu/aggregate.cu:17-438 and
+// src/cpu/aggregate.c:130-188 of the reference):
+//   1. sizes in shard order: s[perm[i]] = size[gather[i]], unmapped
+//      covering positions are 0;
+//   2. the pre-padding sizes are kept for the shard index;
+//   3. the last chunk of each shard group (n_active * cps_inner positions)
+//      absorbs the padding that rounds the group to the shard alignment;
+//   4. exclusive scan -> byte offsets (offsets[positions] = total);
+//   5. every chunk's bytes are copied to out + offsets[perm[i]].
+// Steps 1-4 run in one CTA per level (a few thousand positions); step 5 is a
+// warp per chunk with aligned 32-bit stores built by funnel shifts, so the
+// byte-granular destination never needs unaligned accesses.
+#include "kernels.hpp"
+
+namespace chucky {
+
+namespace {
+
+constexpr int kScanThreads = 1024;
+
+__device__ __forceinline__ uint64_t block_exclusive_scan(uint64_t v,
+                                                         uint64_t* warp_tot,
+                                                         uint64_t& total)
+{
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  uint64_t x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint64_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o)
+      x += y;
+  }
+  if (lane == 31)
+    warp_tot[wid] = x;
+  __syncthreads();
+  if (wid == 0) {
+    uint64_t t = lane < (blockDim.x >> 5) ? warp_tot[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint64_t y = __shfl_up_sync(0xffffffffu, t, o);
+      if (lane >= o)
+        t += y;
+    }
+    warp_tot[lane] = t; // inclusive prefix of warp totals
+  }
+  __syncthreads();
+  const uint64_t before = wid ? warp_tot[wid - 1] : 0;
+  total = warp_tot[(blockDim.x >> 5) - 1];
+  __syncthreads();
+  return before + x - v;
+}
+
+__global__ void __launch_bounds__(kScanThreads)
+agg_layout_k(AggBatch b, uint64_t* scratch, uint64_t scratch_stride)
+{
+  __shared__ uint64_t warp_tot[32];
+  const AggLevel& L = b.lv[blockIdx.x];
+  uint64_t* s = scratch + blockIdx.x * scratch_stride;
+  for (uint64_t p = threadIdx.x; p < L.positions; p += blockDim.x)
+    s[p] = 0;
+  __syncthreads();
+  for (uint64_t i = threadIdx.x; i < L.n; i += blockDim.x)
+    s[L.perm[i]] = b.sizes[L.gather[i]];
+  __syncthreads();
+  for (uint64_t p = threadIdx.x; p < L.positions; p += blockDim.x)
+    L.real_sizes[p] = s[p];
+  if (b.alignment > 0 && L.group > 0) {
+    __syncthreads();
+    for (uint64_t g = threadIdx.x; g < L.positions / L.group;
+         g += blockDim.x) {
+      uint64_t t = 0;
+      for (uint64_t j = 0; j < L.group; ++j)
+        t += s[g * L.group + j];
+      const uint64_t pad = (t + b.alignment - 1) / b.alignment * b.alignment - t;
+      s[g * L.group + L.group - 1] += pad;
+    }
+  }
+  __syncthreads();
+  uint64_t carry = 0;
+  for (uint64_t base = 0; base < L.positions; base += blockDim.x) {
+    const uint64_t p = base + threadIdx.x;
+    const uint64_t v = p < L.positions ? s[p] : 0;
+    uint64_t tile_total;
+    const uint64_t ex = block_exclusive_scan(v, warp_tot, tile_total);
+    if (p < L.positions)
+      L.offsets[p] = carry + ex;
+    carry += tile_total;
+  }
+  if (threadIdx.x == 0)
+    L.offsets[L.positions] = carry;
+}
+
+// Copy `n` bytes from 4-byte aligned `src` to byte address `dst` with one
+// warp.  Full destination words are assembled from two aligned source words.
+__device__ void warp_copy(uint8_t* dst, const uint8_t* src, uint64_t n)
+{
+  const int lane = threadIdx.x & 31;
+  const uint64_t lead = (4 - (uintptr_t(dst) & 3)) & 3;
+  const uint64_t head = n < lead ? n : lead;
+  if (lane < head)
+    dst[lane] = src[lane];
+  const uint64_t body = (n - head) & ~uint64_t(3);
+  uint32_t* d = reinterpret_cast<uint32_t*>(dst + head);
+  const uint32_t* s = reinterpret_cast<const uint32_t*>(src);
+  const unsigned sh = unsigned(head) * 8; // source starts `head` bytes in
+  for (uint64_t w = lane; w < body / 4; w += 32) {
+    if (sh == 0)
+      d[w] = s[w];
+    else
+      d[w] = __funnelshift_r(s[w], s[w + 1], sh);
+  }
+  const uint64_t done = head + body;
+  if (lane < n - done)
+    dst[done + lane] = src[done + lane];
+}
+
+__global__ void __launch_bounds__(128)
+agg_gather_k(AggBatch b, uint64_t total_warps)
+{
+  const uint64_t warp = (blockIdx.x * uint64_t(blockDim.x) + threadIdx.x) >> 5;
+  const uint64_t nwarps = (uint64_t(gridDim.x) * blockDim.x) >> 5;
+  for (uint64_t w = warp; w < total_warps; w += nwarps) {
+    int l = 0;
+    uint64_t i = w;
+    while (l < b.nlevels && i >= b.lv[l].n) {
+      i -= b.lv[l].n;
+      ++l;
+    }
+    if (l >= b.nlevels)
+      return;
+    const AggLevel& L = b.lv[l];
+    const uint32_t c = L.gather[i];
+    const uint64_t n = b.sizes[c];
+    if (n == 0)
+      continue;
+    warp_copy(L.out + L.offsets[L.perm[i]], b.comp + c * b.comp_stride, n);
+  }
+}
+
+__global__ void fill_u64_k(uint64_t* p, uint64_t v, uint64_t n)
+{
+  for (uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; i < n;
+       i += uint64_t(gridDim.x) * blockDim.x)
+    p[i] = v;
+}
+
+} // namespace
+
+cudaError_t launch_aggregate(const AggBatch& b,
+                             uint64_t* scratch,
+                             cudaStream_t st)
+{
+  if (b.nlevels <= 0)
+    return cudaSuccess;
+  uint64_t stride = 0, total = 0;
+  for (int l = 0; l < b.nlevels; ++l) {
+    stride = stride > b.lv[l].positions ? stride : b.lv[l].positions;
+    total += b.lv[l].n;
+  }
+  agg_layout_k<<<b.nlevels, kScanThreads, 0, st>>>(b, scratch, stride);
+  if (total) {
+    const uint64_t blocks = (total + 3) / 4;
+    const int grid = int(blocks < 152 * 32 ? blocks : 152 * 32);
+    agg_gather_k<<<grid, 128, 0, st>>>(b, total);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_fill_u64(uint64_t* p, uint64_t v, uint64_t n, cudaStream_t st)
+{
+  if (!n)
+    return cudaSuccess;
+  const uint64_t blocks = (n + 255) / 256;
+  fill_u64_k<<<int(blocks < 1024 ? blocks : 1024), 256, 0, st>>>(p, v, n);
+  return cudaGetLastError();
+}
+
+} // namespace chucky

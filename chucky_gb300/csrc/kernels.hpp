@@ -1,0 +1,108 @@
+// Host-side launchers of the sm_103a kernels (all asynchronous on `st`).
+#pragma once
+
+#include "common.cuh"
+#include "dtype.h"
+#include "types.lod.h"
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace chucky {
+
+// ---- (a) transpose: row-major epoch -> chunk tiles -------------------------
+
+struct TransposeArgs
+{
+  const uint8_t* src;      // epoch buffer, element 0 = first of the epoch
+  uint8_t* dst;            // epoch slot of the chunk pool
+  uint64_t n;              // elements present (a partial epoch may be short)
+  uint32_t bpe;            // 1, 2, 4 or 8
+  FastDiv width;           // innermost lifted extent (count x chunk)
+  const uint64_t* row_off; // element offset of (row, 0) in the slot
+  const uint64_t* col_off; // element offset of column x within a row
+  int vector_ok;           // 16-byte runs stay contiguous and aligned
+};
+cudaError_t launch_transpose(const TransposeArgs& a, cudaStream_t st);
+
+// ---- (b) LOD pyramid --------------------------------------------------------
+
+// One epoch through the Morton-order path: gather L0 into Morton order,
+// reduce every level from the one below, fold/emit the dim-0 accumulators
+// and scatter the active levels into the chunk slot.
+struct LodMortonArgs
+{
+  int dtype;
+  int reduce_method;
+  int append_method;
+  int nlod;
+  uint64_t fixed_count;
+  const uint64_t* lod_nelem;       // host array [nlod]
+  const uint64_t* level_beg;       // host array [nlod] (element offsets)
+  const uint64_t* accum_beg;       // host array [nlod] (levels >= 1)
+  const uint64_t* d_ends;          // device window ends, levels >= 1
+  const uint64_t* ends_beg;        // host array [nlod] offset into d_ends
+  const uint32_t* d_gather_lut;    // [lod_nelem[0]]
+  const uint64_t* d_gather_fixed;  // [fixed_count]
+  const uint32_t* const* d_chunk_lut;   // host array of device ptrs [nlod]
+  const uint64_t* const* d_chunk_fixed; // host array of device ptrs [nlod]
+};
+
+cudaError_t launch_lod_gather(const LodMortonArgs& a,
+                              const uint8_t* linear,
+                              uint8_t* values,
+                              cudaStream_t st);
+cudaError_t launch_lod_reduce(const LodMortonArgs& a,
+                              uint8_t* values,
+                              cudaStream_t st);
+cudaError_t launch_lod_fold(const LodMortonArgs& a,
+                            int level,
+                            uint32_t count,
+                            const uint8_t* values,
+                            uint8_t* accum,
+                            cudaStream_t st);
+cudaError_t launch_lod_emit(const LodMortonArgs& a,
+                            int level,
+                            uint32_t count,
+                            const uint8_t* accum,
+                            uint8_t* values,
+                            cudaStream_t st);
+cudaError_t launch_lod_to_chunks(const LodMortonArgs& a,
+                                 int level,
+                                 const uint8_t* values,
+                                 uint8_t* slot,
+                                 cudaStream_t st);
+
+// ---- (d) aggregation --------------------------------------------------------
+
+// One level of one batch: n entries (active epochs x chunks per epoch).
+struct AggLevel
+{
+  const uint32_t* gather;  // [n] compressed chunk index
+  const uint32_t* perm;    // [n] covering position in shard order
+  uint64_t n;              // number of mapped chunks
+  uint64_t positions;      // n_active * covering
+  uint64_t group;          // n_active * cps_inner (page-pad unit)
+  uint64_t* offsets;       // [positions + 1] (written)
+  uint64_t* real_sizes;    // [positions] pre-padding sizes (written)
+  uint8_t* out;            // shard-ordered bytes (written)
+};
+
+struct AggBatch
+{
+  const uint8_t* comp;      // compressed chunk slots
+  uint64_t comp_stride;     // bytes between slots
+  const uint64_t* sizes;    // [chunks] compressed sizes
+  uint64_t alignment;       // shard alignment (0 = none)
+  int nlevels;
+  AggLevel lv[32];
+};
+
+// sizes -> shard order -> page pad -> exclusive scan, then gather bytes.
+cudaError_t launch_aggregate(const AggBatch& b,
+                             uint64_t* scratch, // >= max positions
+                             cudaStream_t st);
+
+cudaError_t launch_fill_u64(uint64_t* p, uint64_t v, uint64_t n, cudaStream_t st);
+
+} // namespace chucky

@@ -1,0 +1,942 @@
+// GPU streaming writer: tile_stream_gpu_* (include/stream.gpu.h).
+//
+// One stream object owns, on the current CUDA device:
+//   * two epoch input buffers (row-major, one epoch each) filled by
+//     cudaMemcpyAsync on the copy stream straight from the caller's slice
+//     (pinned, pageable or device memory alike);
+//   * one chunk pool of K epoch slots x all levels, written by the epoch
+//     kernel (transpose, or the LOD pyramid) on the compute stream;
+//   * the compressed pool and sizes, written by the batch encoders;
+//   * per-level shard-order LUTs (planned batch resident on the device).
+// Aggregated shard bytes, offsets and sizes are written by the aggregation
+// kernel directly into one of two mapped pinned host "delivery slots", so
+// nothing is copied back except finished shard data.  The host delivers a
+// batch to the shard sink (index + crc32c + finalize) while the GPU works on
+// the next one.
+//
+// Control flow and contract follow the reference's GPU/CPU streams:
+//   append: src/gpu/stream.c:66-170, src/cpu/stream.c:528-666
+//   flush:  src/gpu/stream.c:173-245, src/cpu/stream.c:668-774
+//   batch:  src/cpu/pipeline.c:113-190, src/gpu/flush.compress_agg.c:224-371
+//   shards: src/zarr/shard_delivery.c:10-204
+#include "plan.hpp"
+#include "stream_internal.hpp"
+
+#include <algorithm>
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <new>
+
+namespace chucky {
+
+uint32_t crc32c_host(const void* data, size_t len);
+
+namespace {
+
+inline uint64_t round_up(uint64_t x, uint64_t a) { return (x + a - 1) / a * a; }
+
+#define CK(expr)                                                               \
+  do {                                                                         \
+    cudaError_t e_ = (expr);                                                   \
+    if (e_ != cudaSuccess) {                                                   \
+      std::fprintf(stderr, "chucky_gb300: %s failed: %s (%s:%d)\n", #expr,     \
+                   cudaGetErrorString(e_), __FILE__, __LINE__);                \
+      return 1;                                                                \
+    }                                                                          \
+  } while (0)
+
+stream_metric mk_metric(const char* name)
+{
+  stream_metric m{};
+  m.name = name;
+  m.best_ms = 1e30f;
+  return m;
+}
+
+void add_metric(stream_metric& m, float ms, double in, double out)
+{
+  m.ms += ms;
+  if (ms < m.best_ms)
+    m.best_ms = ms;
+  m.input_bytes += in;
+  m.output_bytes += out;
+  m.count += 1;
+}
+
+double now_ms()
+{
+  using namespace std::chrono;
+  return duration<double, std::milli>(steady_clock::now().time_since_epoch())
+    .count();
+}
+
+} // namespace
+
+// ---------------------------------------------------------------------------
+// setup / teardown
+// ---------------------------------------------------------------------------
+
+int Stream::timed_begin(cudaStream_t st, stream_metric* m, double in, double out)
+{
+  if (timers_used >= kMaxTimers)
+    resolve_timers(true);
+  Timer& t = timers[timers_used++];
+  t.metric = m;
+  t.in = in;
+  t.out = out;
+  CK(cudaEventRecord(t.a, st));
+  return 0;
+}
+
+int Stream::timed_end(cudaStream_t st)
+{
+  CK(cudaEventRecord(timers[timers_used - 1].b, st));
+  return 0;
+}
+
+void Stream::resolve_timers(bool wait)
+{
+  size_t keep = 0;
+  for (size_t i = 0; i < timers_used; ++i) {
+    Timer& t = timers[i];
+    if (wait)
+      cudaEventSynchronize(t.b);
+    float ms = 0;
+    if (cudaEventElapsedTime(&ms, t.a, t.b) == cudaSuccess) {
+      add_metric(*t.metric, ms, t.in, t.out);
+    } else { // not finished yet: keep it
+      std::swap(timers[keep], timers[i]);
+      ++keep;
+    }
+  }
+  timers_used = keep;
+}
+
+int Stream::init(const tile_stream_configuration* c, shard_sink* sk)
+{
+  cfg = *c;
+  sink = sk;
+  if (plan_stream(&cfg, &P))
+    return 1;
+  layout = P.lv[0].layout;
+  CK(cudaGetDevice(&device));
+  CK(cudaStreamCreateWithFlags(&s_copy, cudaStreamNonBlocking));
+  CK(cudaStreamCreateWithFlags(&s_comp, cudaStreamNonBlocking));
+  for (auto& t : timers) {
+    CK(cudaEventCreate(&t.a));
+    CK(cudaEventCreate(&t.b));
+  }
+  for (int i = 0; i < 2; ++i) {
+    CK(cudaEventCreateWithFlags(&ev_input_ready[i], cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&ev_input_free[i], cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&ev_batch[i], cudaEventDisableTiming));
+    CK(cudaMalloc(&d_epoch[i], round_up(P.epoch_bytes, 256) + 256));
+    CK(cudaEventRecord(ev_input_free[i], s_comp));
+  }
+  const uint64_t pool_bytes = uint64_t(P.K) * P.slot_bytes;
+  CK(cudaMalloc(&d_pool, pool_bytes));
+  CK(cudaMemsetAsync(d_pool, 0, pool_bytes, s_comp));
+  const uint64_t nchunks = uint64_t(P.K) * P.total_chunks;
+  CK(cudaMalloc(&d_sizes, nchunks * sizeof(uint64_t)));
+  if (cfg.codec.id == CODEC_NONE) {
+    comp_stride = layout.chunk_stride * P.bpe;
+    CK(launch_fill_u64(d_sizes, P.chunk_bytes, nchunks, s_comp));
+  } else {
+    comp_stride = round_up(P.max_out, 16);
+    CK(cudaMalloc(&d_comp, nchunks * comp_stride + 64));
+    if (codec_init())
+      return 1;
+  }
+  if (setup_transpose() || setup_lod() || setup_aggregate())
+    return 1;
+
+  metrics.memcpy = mk_metric("memcpy");
+  metrics.h2d = mk_metric("h2d");
+  metrics.scatter = mk_metric("scatter");
+  metrics.compress = mk_metric("compress");
+  metrics.aggregate = mk_metric("aggregate");
+  metrics.d2h = mk_metric("d2h");
+  metrics.sink = mk_metric("sink");
+  if (P.multiscale) {
+    metrics.lod_gather = mk_metric("lod_gather");
+    metrics.lod_reduce = mk_metric("lod_reduce");
+    metrics.lod_append_fold = mk_metric("lod_append_fold");
+    metrics.lod_morton_chunk = mk_metric("lod_morton");
+  }
+  max_cursor = P.max_cursor;
+  CK(cudaStreamSynchronize(s_comp));
+  return 0;
+}
+
+int Stream::setup_transpose()
+{
+  if (P.multiscale)
+    return 0;
+  const tile_stream_layout& L = layout;
+  const int r = L.lifted_rank;
+  const uint64_t cs = L.lifted_shape[r - 1];
+  const uint64_t width = L.lifted_shape[r - 2] * cs;
+  const uint64_t rows = L.epoch_elements / width;
+  std::vector<uint64_t> row(rows), col(width);
+  for (uint64_t x = 0; x < width; ++x)
+    col[x] = (x / cs) * uint64_t(L.lifted_strides[r - 2]) +
+             (x % cs) * uint64_t(L.lifted_strides[r - 1]);
+  for (uint64_t y = 0; y < rows; ++y)
+    row[y] = ravel(r - 2, L.lifted_shape, L.lifted_strides, y);
+  CK(cudaMalloc(&d_row_off, rows * sizeof(uint64_t)));
+  CK(cudaMalloc(&d_col_off, width * sizeof(uint64_t)));
+  CK(cudaMemcpy(d_row_off, row.data(), rows * 8, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(d_col_off, col.data(), width * 8, cudaMemcpyHostToDevice));
+  tr.width = FastDiv(width);
+  tr.row_off = d_row_off;
+  tr.col_off = d_col_off;
+  tr.bpe = uint32_t(P.bpe);
+  tr.vector_ok = L.lifted_strides[r - 1] == 1 && (cs * P.bpe) % 16 == 0 &&
+                 16 % P.bpe == 0;
+  return 0;
+}
+
+int Stream::setup_lod()
+{
+  if (!P.multiscale)
+    return 0;
+  const int nlod = P.nlod;
+  uint64_t total_values = 0, total_accum = 0;
+  for (int l = 0; l < nlod; ++l) {
+    lod_nelem[l] = P.lv[l].lod_nelem;
+    level_beg[l] = total_values;
+    total_values += P.fixed_count * P.lv[l].lod_nelem;
+    if (l >= 1) {
+      accum_beg[l] = total_accum;
+      total_accum += P.fixed_count * P.lv[l].lod_nelem;
+    }
+    ends_beg[l] = l >= 1 ? P.lod_end[l - 1] - P.lod_end[0] : 0;
+  }
+  CK(cudaMalloc(&d_values, total_values * P.bpe + 16));
+  if (P.append_downsample && total_accum)
+    CK(cudaMalloc(&d_accum, total_accum * P.bpe + 16));
+  if (!P.ends.empty()) {
+    CK(cudaMalloc(&d_ends, P.ends.size() * 8));
+    CK(cudaMemcpy(d_ends, P.ends.data(), P.ends.size() * 8,
+                  cudaMemcpyHostToDevice));
+  }
+
+  // L0 gather LUT over the row-major epoch (src/cpu/lod.cpp:181-239).
+  uint64_t stride[HALF_MAX_RANK];
+  stride[P.rank - 1] = 1;
+  for (int d = P.rank - 2; d >= 0; --d)
+    stride[d] = stride[d + 1] * P.lv[0].shape[d + 1];
+  {
+    const uint64_t n0 = P.lv[0].lod_nelem;
+    std::vector<uint32_t> lut(n0);
+    std::vector<uint64_t> fixed(P.fixed_count);
+    uint64_t shp[LOD_MAX_NDIM];
+    for (int k = 0; k < P.lod_ndim; ++k)
+      shp[k] = P.lv[0].shape[P.lod_to_dim[k]];
+    for (uint64_t g = 0; g < n0; ++g) {
+      uint64_t c[LOD_MAX_NDIM], r = g, off = 0;
+      for (int k = P.lod_ndim - 1; k >= 0; --k) {
+        c[k] = r % shp[k];
+        r /= shp[k];
+        off += c[k] * stride[P.lod_to_dim[k]];
+      }
+      lut[morton_rank(P.lod_ndim, shp, c, 0)] = uint32_t(off);
+    }
+    for (uint64_t b = 0; b < P.fixed_count; ++b) {
+      uint64_t r = b, off = 0;
+      for (int k = P.fixed_ndim - 1; k >= 0; --k) {
+        off += (r % P.fixed_shape[k]) * stride[P.fixed_to_dim[k]];
+        r /= P.fixed_shape[k];
+      }
+      fixed[b] = off;
+    }
+    CK(cudaMalloc(&d_gather_lut, n0 * 4));
+    CK(cudaMalloc(&d_gather_fixed, P.fixed_count * 8));
+    CK(cudaMemcpy(d_gather_lut, lut.data(), n0 * 4, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(d_gather_fixed, fixed.data(), P.fixed_count * 8,
+                  cudaMemcpyHostToDevice));
+  }
+  // Morton -> chunk LUTs per level (src/cpu/lod.cpp:318-352,
+  // src/cpu/pipeline.c:373-398).
+  for (int l = 0; l < nlod; ++l) {
+    const tile_stream_layout& L = P.lv[l].layout;
+    const uint64_t n = P.lv[l].lod_nelem;
+    std::vector<uint32_t> lut(n);
+    std::vector<uint64_t> fixed(P.fixed_count);
+    uint64_t shp[LOD_MAX_NDIM];
+    for (int k = 0; k < P.lod_ndim; ++k)
+      shp[k] = P.lv[l].shape[P.lod_to_dim[k]];
+    for (uint64_t g = 0; g < n; ++g) {
+      uint64_t c[LOD_MAX_NDIM], r = g;
+      int64_t off = 0;
+      for (int k = P.lod_ndim - 1; k >= 0; --k) {
+        c[k] = r % shp[k];
+        r /= shp[k];
+        const int d = P.lod_to_dim[k];
+        const uint64_t cs = L.lifted_shape[2 * d + 1];
+        off += int64_t(c[k] / cs) * L.lifted_strides[2 * d] +
+               int64_t(c[k] % cs) * L.lifted_strides[2 * d + 1];
+      }
+      lut[morton_rank(P.lod_ndim, shp, c, 0)] = uint32_t(off);
+    }
+    for (uint64_t b = 0; b < P.fixed_count; ++b) {
+      uint64_t r = b;
+      int64_t off = 0;
+      for (int k = P.fixed_ndim - 1; k >= 0; --k) {
+        const uint64_t coord = r % P.fixed_shape[k];
+        r /= P.fixed_shape[k];
+        const int d = P.fixed_to_dim[k];
+        const uint64_t cs = L.lifted_shape[2 * d + 1];
+        off += int64_t(coord / cs) * L.lifted_strides[2 * d] +
+               int64_t(coord % cs) * L.lifted_strides[2 * d + 1];
+      }
+      fixed[b] = uint64_t(off) + P.lv[l].chunk_offset * L.chunk_stride;
+    }
+    CK(cudaMalloc(&d_chunk_lut[l], n * 4));
+    CK(cudaMalloc(&d_chunk_fixed[l], P.fixed_count * 8));
+    CK(cudaMemcpy(d_chunk_lut[l], lut.data(), n * 4, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(d_chunk_fixed[l], fixed.data(), P.fixed_count * 8,
+                  cudaMemcpyHostToDevice));
+  }
+  lod.dtype = cfg.dtype;
+  lod.reduce_method = cfg.reduce_method;
+  lod.append_method = cfg.append_reduce_method;
+  lod.nlod = nlod;
+  lod.fixed_count = P.fixed_count;
+  lod.lod_nelem = lod_nelem;
+  lod.level_beg = level_beg;
+  lod.accum_beg = accum_beg;
+  lod.d_ends = d_ends;
+  lod.ends_beg = ends_beg;
+  lod.d_gather_lut = d_gather_lut;
+  lod.d_gather_fixed = d_gather_fixed;
+  lod.d_chunk_lut = d_chunk_lut;
+  lod.d_chunk_fixed = d_chunk_fixed;
+  return 0;
+}
+
+// Shard-order LUTs of `n_active` epochs of level l read from pool epochs
+// `eps` (src/stream/types.aggregate.c:28-62).
+void Stream::build_luts(int l,
+                        uint32_t n_active,
+                        const uint32_t* eps,
+                        uint32_t* gather,
+                        uint32_t* perm) const
+{
+  const LevelPlan& V = P.lv[l];
+  const uint64_t M = V.layout.chunks_per_epoch, cpi = V.cps_inner;
+  const uint64_t nsh = V.covering / cpi;
+  for (uint32_t a = 0; a < n_active; ++a)
+    for (uint64_t j = 0; j < M; ++j) {
+      const uint64_t i = uint64_t(a) * M + j;
+      gather[i] = uint32_t(eps[a] * P.total_chunks + V.chunk_offset + j);
+      const uint64_t pos = ravel(V.agg_rank, V.agg_shape, V.agg_strides, j);
+      perm[i] = uint32_t(((pos / cpi) % nsh) * n_active * cpi + pos % cpi +
+                         a * cpi);
+    }
+}
+
+int Stream::setup_aggregate()
+{
+  uint64_t max_positions = 0;
+  for (int l = 0; l < P.nlod; ++l) {
+    const LevelPlan& V = P.lv[l];
+    const uint32_t slots = std::max<uint32_t>(V.batch_active, 1);
+    // the drain batch of a level may exceed its planned count only when
+    // planned is 0, so max(planned, 1) epochs bound every batch
+    const uint32_t cap_epochs = std::max<uint32_t>(slots, 1);
+    const uint64_t M = V.layout.chunks_per_epoch;
+    const uint64_t lut_n = uint64_t(cap_epochs) * M;
+    lut_cap[l] = cap_epochs;
+    CK(cudaMalloc(&d_gather[l], lut_n * 4));
+    CK(cudaMalloc(&d_perm[l], lut_n * 4));
+    CK(cudaMallocHost(&h_lut_stage[l], 2 * lut_n * 4));
+    CK(cudaMalloc(&d_gather_tmp[l], lut_n * 4));
+    CK(cudaMalloc(&d_perm_tmp[l], lut_n * 4));
+    planned_count[l] = V.batch_active;
+    if (V.batch_active) {
+      std::vector<uint32_t> eps(V.batch_active), g(lut_n), pm(lut_n);
+      for (uint32_t a = 0; a < V.batch_active; ++a)
+        eps[a] = (a + 1) * V.period - 1;
+      build_luts(l, V.batch_active, eps.data(), g.data(), pm.data());
+      CK(cudaMemcpy(d_gather[l], g.data(), lut_n * 4, cudaMemcpyHostToDevice));
+      CK(cudaMemcpy(d_perm[l], pm.data(), lut_n * 4, cudaMemcpyHostToDevice));
+    }
+    const uint64_t positions = uint64_t(cap_epochs) * V.covering;
+    max_positions = std::max(max_positions, positions);
+    const uint64_t nshards = V.covering / V.cps_inner;
+    const uint64_t sa = cfg.shard_alignment;
+    const uint64_t data = uint64_t(cap_epochs) * M * P.max_out +
+                          (sa ? (nshards + 1) * sa : 0) + 64;
+    for (int s = 0; s < 2; ++s) {
+      DeliverySlot::Level& D = slot[s].lv[l];
+      D.positions_cap = positions;
+      D.data_cap = data;
+      CK(cudaHostAlloc(&D.offsets, (positions + 1) * 8, cudaHostAllocMapped));
+      CK(cudaHostAlloc(&D.real_sizes, positions * 8 + 8, cudaHostAllocMapped));
+      CK(cudaHostAlloc(&D.data, data, cudaHostAllocMapped));
+    }
+    // shard state (src/zarr/shard_delivery.c:10-34)
+    Shards& S = shards[l];
+    S.sh.resize(V.shard_inner_count);
+    for (auto& sh : S.sh)
+      sh.index.assign(2 * V.cps_total, ~uint64_t(0));
+  }
+  CK(cudaMalloc(&d_agg_scratch, (max_positions + 1) * 8 * size_t(P.nlod)));
+  return 0;
+}
+
+void Stream::release()
+{
+  if (s_comp)
+    cudaStreamSynchronize(s_comp);
+  if (s_copy)
+    cudaStreamSynchronize(s_copy);
+  codec_release();
+  for (int i = 0; i < 2; ++i) {
+    cudaFree(d_epoch[i]);
+    if (ev_input_ready[i])
+      cudaEventDestroy(ev_input_ready[i]);
+    if (ev_input_free[i])
+      cudaEventDestroy(ev_input_free[i]);
+    if (ev_batch[i])
+      cudaEventDestroy(ev_batch[i]);
+    for (int l = 0; l < LOD_MAX_LEVELS; ++l) {
+      cudaFreeHost(slot[i].lv[l].offsets);
+      cudaFreeHost(slot[i].lv[l].real_sizes);
+      cudaFreeHost(slot[i].lv[l].data);
+    }
+  }
+  for (auto& t : timers) {
+    if (t.a)
+      cudaEventDestroy(t.a);
+    if (t.b)
+      cudaEventDestroy(t.b);
+  }
+  cudaFree(d_pool);
+  cudaFree(d_comp);
+  cudaFree(d_sizes);
+  cudaFree(d_row_off);
+  cudaFree(d_col_off);
+  cudaFree(d_values);
+  cudaFree(d_accum);
+  cudaFree(d_ends);
+  cudaFree(d_gather_lut);
+  cudaFree(d_gather_fixed);
+  cudaFree(d_agg_scratch);
+  for (int l = 0; l < LOD_MAX_LEVELS; ++l) {
+    cudaFree(d_chunk_lut[l]);
+    cudaFree(d_chunk_fixed[l]);
+    cudaFree(d_gather[l]);
+    cudaFree(d_perm[l]);
+    cudaFree(d_gather_tmp[l]);
+    cudaFree(d_perm_tmp[l]);
+    cudaFreeHost(h_lut_stage[l]);
+  }
+  if (s_copy)
+    cudaStreamDestroy(s_copy);
+  if (s_comp)
+    cudaStreamDestroy(s_comp);
+}
+
+// ---------------------------------------------------------------------------
+// epochs
+// ---------------------------------------------------------------------------
+
+uint8_t* Stream::pool_slot(uint32_t e) const
+{
+  return d_pool + uint64_t(e) * P.slot_bytes;
+}
+
+int Stream::run_epoch(uint64_t present)
+{
+  const int b = in_buf;
+  CK(cudaEventRecord(ev_input_ready[b], s_copy));
+  CK(cudaStreamWaitEvent(s_comp, ev_input_ready[b], 0));
+  if (present < layout.epoch_elements) // partial final epoch: fill value 0
+    CK(cudaMemsetAsync(d_epoch[b] + present * P.bpe, 0,
+                       (layout.epoch_elements - present) * P.bpe, s_comp));
+  uint8_t* slot_ptr = pool_slot(accumulated);
+  uint32_t mask = 1;
+  if (!P.multiscale) {
+    TransposeArgs a = tr;
+    a.src = d_epoch[b];
+    a.dst = slot_ptr;
+    a.n = layout.epoch_elements;
+    if (timed_begin(s_comp, &metrics.scatter, double(P.epoch_bytes),
+                    double(P.epoch_bytes)))
+      return 1;
+    CK(launch_transpose(a, s_comp));
+    if (timed_end(s_comp))
+      return 1;
+  } else {
+    const double vb = double(P.fixed_count * P.lv[0].lod_nelem * P.bpe);
+    if (timed_begin(s_comp, &metrics.lod_gather, vb, vb))
+      return 1;
+    CK(launch_lod_gather(lod, d_epoch[b], d_values, s_comp));
+    if (timed_end(s_comp))
+      return 1;
+    if (timed_begin(s_comp, &metrics.lod_reduce, vb, 0))
+      return 1;
+    CK(launch_lod_reduce(lod, d_values, s_comp));
+    if (timed_end(s_comp))
+      return 1;
+    mask = (P.append_downsample && d_accum) ? 1u
+                                             : uint32_t((1ull << P.nlod) - 1);
+    if (P.append_downsample && d_accum) {
+      if (timed_begin(s_comp, &metrics.lod_append_fold, 0, 0))
+        return 1;
+      for (int l = 1; l < P.nlod; ++l)
+        CK(launch_lod_fold(lod, l, counts[l], d_values, d_accum, s_comp));
+      for (int l = 1; l < P.nlod; ++l) {
+        counts[l]++;
+        if (counts[l] >= (1u << l)) {
+          CK(launch_lod_emit(lod, l, counts[l], d_accum, d_values, s_comp));
+          counts[l] = 0;
+          mask |= 1u << l;
+        }
+      }
+      if (timed_end(s_comp))
+        return 1;
+    }
+    if (timed_begin(s_comp, &metrics.lod_morton_chunk, 0, double(P.slot_bytes)))
+      return 1;
+    for (int l = 0; l < P.nlod; ++l)
+      if (mask >> l & 1)
+        CK(launch_lod_to_chunks(lod, l, d_values, slot_ptr, s_comp));
+    if (timed_end(s_comp))
+      return 1;
+  }
+  CK(cudaEventRecord(ev_input_free[b], s_comp));
+  in_buf ^= 1;
+  in_fill = 0;
+  if (accumulated >= MAX_BATCH_EPOCHS)
+    return 1;
+  masks[accumulated++] = mask;
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// batches
+// ---------------------------------------------------------------------------
+
+int Stream::kick_batch(uint32_t n_epochs, const uint32_t* epoch_masks)
+{
+  const int si = next_slot;
+  DeliverySlot& S = slot[si];
+  if (S.busy && deliver(si)) // cannot happen with drain-before-kick
+    return 1;
+  const uint64_t nchunks = uint64_t(n_epochs) * P.total_chunks;
+  const uint8_t* comp = d_pool;
+  if (cfg.codec.id != CODEC_NONE) {
+    if (timed_begin(s_comp, &metrics.compress, double(nchunks * P.chunk_bytes),
+                    0))
+      return 1;
+    if (codec_compress(nchunks))
+      return 1;
+    if (timed_end(s_comp))
+      return 1;
+    comp = d_comp;
+  }
+  AggBatch ab{};
+  ab.comp = comp;
+  ab.comp_stride = comp_stride;
+  ab.sizes = d_sizes;
+  ab.alignment = cfg.shard_alignment;
+  S.n_levels = 0;
+  for (int l = 0; l < P.nlod; ++l) {
+    uint32_t eps[MAX_BATCH_EPOCHS], na = 0;
+    for (uint32_t e = 0; e < n_epochs; ++e)
+      if (epoch_masks[e] >> l & 1)
+        eps[na++] = e;
+    S.active[l] = na;
+    if (!na)
+      continue;
+    const LevelPlan& V = P.lv[l];
+    if (na > lut_cap[l])
+      return 1;
+    bool planned = na == planned_count[l];
+    for (uint32_t a = 0; planned && a < na; ++a)
+      planned = eps[a] == (a + 1) * V.period - 1;
+    const uint32_t* g = d_gather[l];
+    const uint32_t* pm = d_perm[l];
+    const uint64_t n = uint64_t(na) * V.layout.chunks_per_epoch;
+    if (!planned) {
+      // lut staging is reused: wait for the previous upload from it
+      CK(cudaStreamSynchronize(s_comp));
+      uint32_t* hg = h_lut_stage[l];
+      uint32_t* hp = h_lut_stage[l] + n;
+      build_luts(l, na, eps, hg, hp);
+      CK(cudaMemcpyAsync(d_gather_tmp[l], hg, n * 4, cudaMemcpyHostToDevice,
+                         s_comp));
+      CK(cudaMemcpyAsync(d_perm_tmp[l], hp, n * 4, cudaMemcpyHostToDevice,
+                         s_comp));
+      g = d_gather_tmp[l];
+      pm = d_perm_tmp[l];
+    }
+    AggLevel& A = ab.lv[ab.nlevels++];
+    A.gather = g;
+    A.perm = pm;
+    A.n = n;
+    A.positions = uint64_t(na) * V.covering;
+    A.group = uint64_t(na) * V.cps_inner;
+    DeliverySlot::Level& D = S.lv[l];
+    A.offsets = D.offsets;
+    A.real_sizes = D.real_sizes;
+    A.out = D.data;
+    S.level_of[S.n_levels++] = l;
+  }
+  // zero-copy writes handed to the sink from this slot must have retired
+  // before the slot is overwritten (src/writer.h:44-49)
+  if (sink->wait_fence)
+    for (int k = 0; k < S.n_levels; ++k)
+      sink->wait_fence(sink, uint8_t(S.level_of[k]), S.fence[S.level_of[k]]);
+  if (timed_begin(s_comp, &metrics.aggregate, 0, 0))
+    return 1;
+  CK(launch_aggregate(ab, d_agg_scratch, s_comp));
+  if (timed_end(s_comp))
+    return 1;
+  CK(cudaEventRecord(ev_batch[si], s_comp));
+  S.busy = 1;
+  S.seq = ++batch_seq;
+  next_slot ^= 1;
+  return 0;
+}
+
+// Write one delivered batch to the shard sink
+// (src/zarr/shard_delivery.c:105-204).
+int Stream::deliver(int si)
+{
+  DeliverySlot& S = slot[si];
+  if (!S.busy)
+    return 0;
+  CK(cudaEventSynchronize(ev_batch[si]));
+  S.busy = 0;
+  resolve_timers(false);
+  const double t0 = now_ms();
+  uint64_t bytes_out = 0;
+  const uint64_t sa = cfg.shard_alignment;
+  for (int k = 0; k < S.n_levels; ++k) {
+    const int l = S.level_of[k];
+    const uint32_t n_active = S.active[l];
+    const LevelPlan& V = P.lv[l];
+    const DeliverySlot::Level& D = S.lv[l];
+    const uint64_t cpi = V.cps_inner;
+    Shards& SS = shards[l];
+    uint32_t a = 0;
+    while (a < n_active) {
+      const uint32_t left = uint32_t(V.cps_append - SS.epoch_in_shard);
+      const uint32_t run = std::min(left, n_active - a);
+      for (uint64_t s = 0; s < V.shard_inner_count; ++s) {
+        Shard& sh = SS.sh[s];
+        if (!sh.w) {
+          sh.w = sink->open(sink, uint8_t(l),
+                            SS.shard_epoch * V.shard_inner_count + s);
+          if (!sh.w)
+            return 1;
+        }
+        const uint64_t j0 = s * n_active * cpi + uint64_t(a) * cpi;
+        const uint64_t j1 = j0 + uint64_t(run) * cpi;
+        const uint64_t nbytes = D.offsets[j1] - D.offsets[j0];
+        const uint64_t wbytes = sa ? round_up(nbytes, sa) : nbytes;
+        if (nbytes > 0) {
+          const uint8_t* src = D.data + D.offsets[j0];
+          const bool aligned = sa == 0 || uintptr_t(src) % sa == 0;
+          int rc;
+          if (aligned && sh.w->write_direct)
+            rc = sh.w->write_direct(sh.w, sh.cursor, src, src + wbytes);
+          else
+            rc = sh.w->write(sh.w, sh.cursor, src, src + wbytes);
+          if (rc)
+            return 1;
+          bytes_out += wbytes;
+        }
+        for (uint32_t r = 0; r < run; ++r) {
+          const uint64_t eis = SS.epoch_in_shard + r;
+          const uint64_t js = j0 + uint64_t(r) * cpi;
+          for (uint64_t j = js; j < js + cpi; ++j)
+            if (D.real_sizes[j] > 0) {
+              const uint64_t slot_idx = eis * cpi + (j - js);
+              sh.index[2 * slot_idx] = sh.cursor + (D.offsets[j] - D.offsets[j0]);
+              sh.index[2 * slot_idx + 1] = D.real_sizes[j];
+            }
+        }
+        sh.cursor += wbytes;
+      }
+      SS.epoch_in_shard += run;
+      a += run;
+      if (SS.epoch_in_shard >= V.cps_append && finalize_level(l))
+        return 1;
+    }
+    if (sink->record_fence) {
+      io_done[l] = sink->record_fence(sink, uint8_t(l));
+      S.fence[l] = io_done[l];
+    }
+  }
+  add_metric(metrics.sink, float(now_ms() - t0), 0, double(bytes_out));
+  return 0;
+}
+
+// Index (u64 offset, nbytes pairs; empty = all ones) + crc32c, then finalize
+// every open shard of the level (src/zarr/shard_delivery.c:36-102).
+int Stream::finalize_level(int l)
+{
+  const LevelPlan& V = P.lv[l];
+  Shards& SS = shards[l];
+  const uint64_t sa = cfg.shard_alignment;
+  int err = 0;
+  for (auto& sh : SS.sh) {
+    if (!sh.w)
+      continue;
+    const uint64_t nidx = V.cps_total * 16, total = nidx + 4;
+    const uint64_t wb = sa ? round_up(total, sa) : total;
+    const uint64_t pad = wb - total;
+    std::vector<uint8_t> buf(wb, 0);
+    std::memcpy(buf.data() + pad, sh.index.data(), nidx);
+    const uint32_t crc = crc32c_host(buf.data() + pad, nidx);
+    std::memcpy(buf.data() + pad + nidx, &crc, 4);
+    if (sh.w->write(sh.w, sh.cursor, buf.data(), buf.data() + wb))
+      err = 1;
+    if (sh.w->finalize(sh.w))
+      err = 1;
+    sh.w = nullptr;
+    sh.cursor = 0;
+    std::fill(sh.index.begin(), sh.index.end(), ~uint64_t(0));
+  }
+  SS.epoch_in_shard = 0;
+  SS.shard_epoch++;
+  return err;
+}
+
+int Stream::drain_all()
+{
+  for (int k = 0; k < 2; ++k) {
+    // deliver in submission order
+    int first = -1;
+    for (int i = 0; i < 2; ++i)
+      if (slot[i].busy && (first < 0 || slot[i].seq < slot[first].seq))
+        first = i;
+    if (first < 0)
+      break;
+    if (deliver(first))
+      return 1;
+  }
+  return 0;
+}
+
+int Stream::batch_boundary()
+{
+  // the previous batch is delivered while this one runs on the GPU
+  const int prev = next_slot ^ 1;
+  if (kick_batch(accumulated, masks))
+    return 1;
+  accumulated = 0;
+  if (slot[prev].busy && slot[prev].seq < batch_seq)
+    return deliver(prev);
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// writer vtable
+// ---------------------------------------------------------------------------
+
+writer_result Stream::append(slice in)
+{
+  if (flushed)
+    return writer_finished_at(in.beg, in.end);
+  const uint8_t* src = static_cast<const uint8_t*>(in.beg);
+  const uint8_t* end = static_cast<const uint8_t*>(in.end);
+  const uint64_t ee = layout.epoch_elements;
+  const double t0 = now_ms();
+  uint64_t copied = 0;
+  while (src < end) {
+    if (max_cursor > 0 && cursor >= max_cursor) {
+      cudaStreamSynchronize(s_copy);
+      if (flush_all())
+        return writer_error_at(src, end);
+      return writer_finished_at(src, end);
+    }
+    uint64_t n = std::min<uint64_t>(ee - cursor % ee,
+                                    uint64_t(end - src) / P.bpe);
+    if (max_cursor > 0)
+      n = std::min<uint64_t>(n, max_cursor - cursor);
+    if (n == 0)
+      break;
+    if (in_fill == 0 &&
+        cudaStreamWaitEvent(s_copy, ev_input_free[in_buf], 0) != cudaSuccess)
+      return writer_error_at(src, end);
+    if (cudaMemcpyAsync(d_epoch[in_buf] + in_fill * P.bpe, src, n * P.bpe,
+                        cudaMemcpyDefault, s_copy) != cudaSuccess)
+      return writer_error_at(src, end);
+    copied += n * P.bpe;
+    in_fill += n;
+    cursor += n;
+    src += n * P.bpe;
+    if (cursor % ee == 0) {
+      if (run_epoch(ee))
+        return writer_error_at(src, end);
+      if (accumulated == P.K && batch_boundary())
+        return writer_error_at(src, end);
+    }
+  }
+  // the caller's buffer is only borrowed for the duration of the call
+  if (cudaStreamSynchronize(s_copy) != cudaSuccess)
+    return writer_error_at(src, end);
+  if (copied)
+    add_metric(metrics.h2d, float(now_ms() - t0), double(copied),
+               double(copied));
+  return writer_result{ 0, { src, end } };
+}
+
+int Stream::flush_all()
+{
+  const uint64_t ee = layout.epoch_elements;
+  if (cursor % ee != 0 && run_epoch(cursor % ee))
+    return 1;
+  if (accumulated > 0 && batch_boundary())
+    return 1;
+  if (drain_all())
+    return 1;
+  if (P.append_downsample && d_accum) {
+    uint32_t drain = 0;
+    for (int l = 1; l < P.nlod; ++l)
+      if (counts[l] > 0) {
+        CK(launch_lod_emit(lod, l, counts[l], d_accum, d_values, s_comp));
+        counts[l] = 0;
+        CK(launch_lod_to_chunks(lod, l, d_values, pool_slot(0), s_comp));
+        drain |= 1u << l;
+      }
+    if (drain) {
+      uint32_t m[1] = { drain };
+      if (kick_batch(1, m) || drain_all())
+        return 1;
+    }
+  }
+  for (int l = 0; l < P.nlod; ++l) {
+    if (sink->wait_fence)
+      sink->wait_fence(sink, uint8_t(l), io_done[l]);
+    if (shards[l].epoch_in_shard > 0 && finalize_level(l))
+      return 1;
+  }
+  if (sink->update_append) {
+    const dimension* dims = cfg.dimensions;
+    for (int l = 0; l < P.nlod; ++l) {
+      uint64_t sizes[HALF_MAX_RANK] = {};
+      uint64_t inner = 1;
+      for (int d = 1; d < P.rank; ++d)
+        inner *= dims[d].size;
+      for (int d = 1; d < P.na; ++d)
+        sizes[d] = dims[d].size;
+      uint64_t d0 = inner ? cursor / inner : 0;
+      if (l > 0 && P.append_downsample)
+        d0 = (d0 + ((uint64_t(1) << l) - 1)) >> l;
+      sizes[0] = d0;
+      if (sink->update_append(sink, uint8_t(l), P.na, sizes))
+        return 1;
+    }
+  }
+  resolve_timers(true);
+  return 0;
+}
+
+writer_result Stream::flush()
+{
+  if (flushed)
+    return writer_finished_at(nullptr, nullptr);
+  const int rc = flush_all();
+  flushed = 1;
+  return rc ? writer_error() : writer_ok();
+}
+
+} // namespace chucky
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+
+using chucky::Stream;
+
+static writer_result
+vt_append(writer* w, slice s)
+{
+  return reinterpret_cast<tile_stream_gpu*>(w)->impl.append(s);
+}
+
+static writer_result
+vt_flush(writer* w)
+{
+  return reinterpret_cast<tile_stream_gpu*>(w)->impl.flush();
+}
+
+extern "C" tile_stream_gpu*
+tile_stream_gpu_create(const tile_stream_configuration* config,
+                       shard_sink* sink)
+{
+  if (!config || !sink || !sink->open)
+    return nullptr;
+  tile_stream_gpu* s = new (std::nothrow) tile_stream_gpu();
+  if (!s)
+    return nullptr;
+  s->w.append = vt_append;
+  s->w.flush = vt_flush;
+  if (s->impl.init(config, sink)) {
+    s->impl.release();
+    delete s;
+    return nullptr;
+  }
+  return s;
+}
+
+extern "C" void
+tile_stream_gpu_destroy(tile_stream_gpu* s)
+{
+  if (!s)
+    return;
+  s->impl.release();
+  delete s;
+}
+
+extern "C" stream_metrics
+tile_stream_gpu_get_metrics(const tile_stream_gpu* s)
+{
+  const_cast<tile_stream_gpu*>(s)->impl.resolve_timers(false);
+  return s->impl.metrics;
+}
+
+extern "C" const tile_stream_layout*
+tile_stream_gpu_layout(const tile_stream_gpu* s)
+{
+  return &s->impl.layout;
+}
+
+extern "C" writer*
+tile_stream_gpu_writer(tile_stream_gpu* s)
+{
+  return &s->w;
+}
+
+extern "C" uint64_t
+tile_stream_gpu_cursor(const tile_stream_gpu* s)
+{
+  return s->impl.cursor;
+}
+
+extern "C" tile_stream_status
+tile_stream_gpu_status(const tile_stream_gpu* s)
+{
+  const Stream& I = s->impl;
+  tile_stream_status st{};
+  st.nlod = I.P.nlod;
+  st.append_downsample = I.P.append_downsample;
+  st.epochs_per_batch = I.P.K;
+  st.max_compressed_size = I.P.max_out;
+  st.dtype = I.cfg.dtype;
+  st.codec = I.cfg.codec;
+  st.codec_batch_size = size_t(I.P.K) * I.P.total_chunks;
+  st.batch_accumulated = I.accumulated;
+  st.pool_current = 0;
+  st.flush_pending = (I.slot[0].busy || I.slot[1].busy) ? 1 : 0;
+  return st;
+}

@@ -1,0 +1,162 @@
+// Internal state of one GPU stream (not part of the C ABI).
+#pragma once
+
+#include "kernels.hpp"
+#include "plan.hpp"
+#include "stream.gpu.h"
+
+#include <cuda_runtime.h>
+#include <vector>
+
+namespace chucky {
+
+struct Shard
+{
+  uint64_t cursor = 0;         // bytes written so far
+  std::vector<uint64_t> index; // 2 * cps_total entries
+  shard_writer* w = nullptr;
+};
+
+struct Shards
+{
+  uint64_t epoch_in_shard = 0;
+  uint64_t shard_epoch = 0;
+  std::vector<Shard> sh;
+};
+
+// Mapped pinned host memory the aggregation kernel writes into.
+struct DeliverySlot
+{
+  struct Level
+  {
+    uint64_t* offsets = nullptr;    // [positions + 1]
+    uint64_t* real_sizes = nullptr; // [positions]
+    uint8_t* data = nullptr;
+    uint64_t positions_cap = 0, data_cap = 0;
+  };
+  Level lv[LOD_MAX_LEVELS];
+  uint32_t active[LOD_MAX_LEVELS] = {};
+  int level_of[LOD_MAX_LEVELS] = {};
+  int n_levels = 0;
+  io_event fence[LOD_MAX_LEVELS] = {};
+  int busy = 0;
+  uint64_t seq = 0;
+};
+
+struct Stream
+{
+  tile_stream_configuration cfg{};
+  shard_sink* sink = nullptr;
+  StreamPlan P;
+  tile_stream_layout layout{};
+  int device = 0;
+  cudaStream_t s_copy = nullptr, s_comp = nullptr;
+
+  // input
+  uint8_t* d_epoch[2] = {};
+  cudaEvent_t ev_input_ready[2] = {}, ev_input_free[2] = {};
+  int in_buf = 0;
+  uint64_t in_fill = 0;
+
+  // chunk pool / compression
+  uint8_t* d_pool = nullptr;
+  uint8_t* d_comp = nullptr;
+  uint64_t* d_sizes = nullptr;
+  uint64_t comp_stride = 0;
+  void* codec_state = nullptr;
+
+  // transpose
+  uint64_t* d_row_off = nullptr;
+  uint64_t* d_col_off = nullptr;
+  TransposeArgs tr{};
+
+  // LOD
+  uint8_t* d_values = nullptr;
+  uint8_t* d_accum = nullptr;
+  uint64_t* d_ends = nullptr;
+  uint32_t* d_gather_lut = nullptr;
+  uint64_t* d_gather_fixed = nullptr;
+  uint32_t* d_chunk_lut[LOD_MAX_LEVELS] = {};
+  uint64_t* d_chunk_fixed[LOD_MAX_LEVELS] = {};
+  uint64_t lod_nelem[LOD_MAX_LEVELS] = {};
+  uint64_t level_beg[LOD_MAX_LEVELS] = {};
+  uint64_t accum_beg[LOD_MAX_LEVELS] = {};
+  uint64_t ends_beg[LOD_MAX_LEVELS] = {};
+  uint32_t counts[LOD_MAX_LEVELS] = {};
+  LodMortonArgs lod{};
+
+  // aggregation
+  uint32_t* d_gather[LOD_MAX_LEVELS] = {};
+  uint32_t* d_perm[LOD_MAX_LEVELS] = {};
+  uint32_t* d_gather_tmp[LOD_MAX_LEVELS] = {};
+  uint32_t* d_perm_tmp[LOD_MAX_LEVELS] = {};
+  uint32_t* h_lut_stage[LOD_MAX_LEVELS] = {};
+  uint32_t lut_cap[LOD_MAX_LEVELS] = {};
+  uint32_t planned_count[LOD_MAX_LEVELS] = {};
+  uint64_t* d_agg_scratch = nullptr;
+  DeliverySlot slot[2];
+  cudaEvent_t ev_batch[2] = {};
+  int next_slot = 0;
+  uint64_t batch_seq = 0;
+
+  // shards
+  Shards shards[LOD_MAX_LEVELS];
+  io_event io_done[LOD_MAX_LEVELS] = {};
+
+  // progress
+  uint64_t cursor = 0, max_cursor = 0;
+  uint32_t accumulated = 0;
+  uint32_t masks[MAX_BATCH_EPOCHS] = {};
+  int flushed = 0;
+
+  // metrics: event pairs resolved lazily
+  struct Timer
+  {
+    cudaEvent_t a = nullptr, b = nullptr;
+    stream_metric* metric = nullptr;
+    double in = 0, out = 0;
+  };
+  static constexpr size_t kMaxTimers = 64;
+  Timer timers[kMaxTimers];
+  size_t timers_used = 0;
+  stream_metrics metrics{};
+
+  int init(const tile_stream_configuration* c, shard_sink* s);
+  void release();
+  int setup_transpose();
+  int setup_lod();
+  int setup_aggregate();
+  void build_luts(int l,
+                  uint32_t n_active,
+                  const uint32_t* eps,
+                  uint32_t* gather,
+                  uint32_t* perm) const;
+  uint8_t* pool_slot(uint32_t e) const;
+  int run_epoch(uint64_t present);
+  int kick_batch(uint32_t n_epochs, const uint32_t* epoch_masks);
+  int batch_boundary();
+  int deliver(int si);
+  int drain_all();
+  int finalize_level(int l);
+  int flush_all();
+  writer_result append(slice in);
+  writer_result flush();
+
+  int codec_init();
+  int codec_compress(uint64_t nchunks);
+  void codec_release();
+
+  int timed_begin(cudaStream_t st, stream_metric* m, double in, double out);
+  int timed_end(cudaStream_t st);
+  void resolve_timers(bool wait);
+};
+
+} // namespace chucky
+
+// The C handle: the writer vtable must come first (the vtable callbacks
+// recover the stream from the writer pointer).
+struct tile_stream_gpu
+{
+  writer w;
+  chucky::Stream impl;
+};

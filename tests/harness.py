@@ -183,3 +183,51 @@ def parse_shard(blob, n_slots, alignment=0):
     buf = C.create_string_buffer(tail[:idx_bytes], idx_bytes)
     ok = lib.oracle_crc32c(buf, idx_bytes) == crc
     return index, ok
+
+
+def run_gpu(cfg, data, pieces=None):
+    """This library's GPU stream on the same input (needs a GPU)."""
+    import chucky_gb300 as cg
+    sink = MemSink()
+    try:
+        s = cg.GpuStream(cfg, sink.base)
+        try:
+            _drive(s.writer, data, pieces)
+            cursor = s.cursor()
+        finally:
+            s.close()
+        return sink.shards(), cursor
+    finally:
+        sink.close()
+
+
+def epoch_elements(cfg):
+    """Elements per epoch, from the oracle's plan."""
+    lib = oracle()
+    sink = MemSink()
+    try:
+        s = lib.oracle_stream_create(C.byref(cfg), sink.base)
+        if not s:
+            raise RuntimeError("invalid config")
+        ee = lib.oracle_stream_layout(s).contents.epoch_elements
+        lib.oracle_stream_destroy(s)
+        return ee
+    finally:
+        sink.close()
+
+
+def diff_shards(a, b):
+    """Human-readable list of differing shard keys."""
+    out = []
+    for k in sorted(set(a) | set(b)):
+        x, y = a.get(k), b.get(k)
+        if x != y:
+            if x is None or y is None:
+                out.append(f"{k}: present only in {'b' if x is None else 'a'}")
+            elif x[0] != y[0]:
+                n = min(len(x[0]), len(y[0]))
+                first = next((i for i in range(n) if x[0][i] != y[0][i]), n)
+                out.append(f"{k}: sizes {len(x[0])}/{len(y[0])} first diff at {first}")
+            else:
+                out.append(f"{k}: finalized {x[1]}/{y[1]}")
+    return out
