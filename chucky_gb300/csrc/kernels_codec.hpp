@@ -1,0 +1,29 @@
+// Batched chunk encoders (LZ4 block, zstd frame).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+namespace chucky {
+
+struct CodecBatch
+{
+  const uint8_t* in;    // first chunk (4-byte aligned)
+  uint64_t in_stride;   // bytes between chunks
+  uint32_t chunk_bytes; // codec input per chunk
+  uint64_t n_chunks;
+  uint8_t* out;         // compressed slots
+  uint64_t out_stride;  // bytes between slots (>= bound)
+  uint64_t* out_sizes;  // [n_chunks] compressed sizes (written)
+  uint32_t segs_per_chunk;
+  int level;
+};
+
+size_t lz4_scratch_bytes(uint64_t n_chunks, uint32_t chunk_bytes);
+cudaError_t launch_lz4(CodecBatch b, void* scratch, cudaStream_t st);
+
+size_t zstd_scratch_bytes(uint64_t n_chunks, uint32_t chunk_bytes);
+cudaError_t launch_zstd(CodecBatch b, void* scratch, cudaStream_t st);
+
+} // namespace chucky

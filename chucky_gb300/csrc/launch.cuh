@@ -1,0 +1,8 @@
+// Kernel launch spelled as a macro so that the encoder sources can also be
+// compiled by the CPU SIMT emulation used in tests (tests/emu).
+#pragma once
+
+#ifndef CHUCKY_LAUNCH
+#define CHUCKY_LAUNCH(kernel, grid, block, smem, stream, ...)                  \
+  kernel<<<(grid), (block), (smem), (stream)>>>(__VA_ARGS__)
+#endif

@@ -23,6 +23,7 @@
 #include "stream_internal.hpp"
 
 #include <algorithm>
+#include <cstddef>
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -136,7 +137,7 @@ int Stream::init(const tile_stream_configuration* c, shard_sink* sk)
     CK(cudaEventRecord(ev_input_free[i], s_comp));
   }
   const uint64_t pool_bytes = uint64_t(P.K) * P.slot_bytes;
-  CK(cudaMalloc(&d_pool, pool_bytes));
+  CK(cudaMalloc(&d_pool, pool_bytes + 256)); // encoders read 8 B past a chunk
   CK(cudaMemsetAsync(d_pool, 0, pool_bytes, s_comp));
   const uint64_t nchunks = uint64_t(P.K) * P.total_chunks;
   CK(cudaMalloc(&d_sizes, nchunks * sizeof(uint64_t)));
@@ -939,4 +940,96 @@ tile_stream_gpu_status(const tile_stream_gpu* s)
   st.pool_current = 0;
   st.flush_pending = (I.slot[0].busy || I.slot[1].busy) ? 1 : 0;
   return st;
+}
+
+extern "C" int
+tile_stream_gpu_restart(tile_stream_gpu* s, shard_sink* sink)
+{
+  if (!s)
+    return 1;
+  Stream& I = s->impl;
+  if (I.cursor != 0 && !I.flushed)
+    return 1;
+  if (cudaStreamSynchronize(I.s_comp) != cudaSuccess ||
+      cudaStreamSynchronize(I.s_copy) != cudaSuccess)
+    return 1;
+  if (sink)
+    I.sink = sink;
+  I.cursor = 0;
+  I.flushed = 0;
+  I.accumulated = 0;
+  I.in_buf = 0;
+  I.in_fill = 0;
+  for (auto& c : I.counts)
+    c = 0;
+  for (int l = 0; l < I.P.nlod; ++l) {
+    chucky::Shards& S = I.shards[l];
+    S.epoch_in_shard = 0;
+    S.shard_epoch = 0;
+    for (auto& sh : S.sh) {
+      sh.cursor = 0;
+      sh.w = nullptr;
+      std::fill(sh.index.begin(), sh.index.end(), ~uint64_t(0));
+    }
+    I.io_done[l] = io_event{};
+  }
+  for (auto& sl : I.slot) {
+    sl.busy = 0;
+    for (auto& f : sl.fence)
+      f = io_event{};
+  }
+  return 0;
+}
+
+namespace {
+
+struct DiscardSink
+{
+  shard_sink base;
+  shard_writer w;
+  uint64_t bytes;
+};
+
+int discard_write(shard_writer* self, uint64_t, const void* b, const void* e)
+{
+  DiscardSink* d = reinterpret_cast<DiscardSink*>(
+    reinterpret_cast<char*>(self) - offsetof(DiscardSink, w));
+  d->bytes += uint64_t(static_cast<const char*>(e) - static_cast<const char*>(b));
+  return 0;
+}
+
+int discard_finalize(shard_writer*)
+{
+  return 0;
+}
+
+shard_writer* discard_open(shard_sink* self, uint8_t, uint64_t)
+{
+  return &reinterpret_cast<DiscardSink*>(self)->w;
+}
+
+} // namespace
+
+extern "C" shard_sink*
+chucky_discard_sink_create(void)
+{
+  DiscardSink* d = new (std::nothrow) DiscardSink{};
+  if (!d)
+    return nullptr;
+  d->base.open = discard_open;
+  d->w.write = discard_write;
+  d->w.finalize = discard_finalize;
+  return &d->base;
+}
+
+extern "C" void
+chucky_discard_sink_destroy(shard_sink* s)
+{
+  delete reinterpret_cast<DiscardSink*>(s);
+}
+
+extern "C" uint64_t
+chucky_discard_sink_bytes(const shard_sink* s)
+{
+  return reinterpret_cast<const DiscardSink*>(s)->bytes;
 }

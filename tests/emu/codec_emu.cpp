@@ -1,0 +1,143 @@
+// Runs the LZ4 and zstd encoder kernels under the CPU SIMT emulation and
+// decodes every chunk with the stock liblz4 / libzstd -- TEST
+// INFRASTRUCTURE ONLY.  Built with AddressSanitizer + UBSan (alignment) when
+// available, so out-of-bounds and misaligned accesses abort with a report.
+//
+// usage: codec_emu <lz4|zstd> <chunk_bytes> <n_chunks> <pattern> <seed>
+#include "simt.hpp"
+
+#include "../../chucky_gb300/csrc/lz4.cu"
+#include "../../chucky_gb300/csrc/zstd.cu"
+
+#include <dlfcn.h>
+#include <string>
+
+using namespace chucky;
+
+static uint64_t rng_state;
+static uint64_t rnd()
+{
+  uint64_t z = (rng_state += 0x9e3779b97f4a7c15ULL);
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ULL;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebULL;
+  return z ^ (z >> 31);
+}
+
+static void fill(uint8_t* p, size_t n, const std::string& pat, size_t chunk)
+{
+  for (size_t i = 0; i < n; ++i) {
+    if (pat == "zeros")
+      p[i] = 0;
+    else if (pat == "random")
+      p[i] = uint8_t(rnd());
+    else if (pat == "ramp")
+      p[i] = uint8_t(i % 251);
+    else if (pat == "xor16") { // u16 (x^y^z)*257 + noise(0..15)
+      const size_t e = i / 2, x = e % 64, y = (e / 64) % 64, z = e / 4096;
+      const uint16_t v = uint16_t(((x ^ y ^ z) * 257 + (rnd() & 15)));
+      p[i] = (i & 1) ? uint8_t(v >> 8) : uint8_t(v);
+    } else { // mixed: per-chunk classes
+      const size_t c = i / chunk;
+      const uint64_t h = (c * 0x9E3779B97F4A7C15ULL) >> 60;
+      if (h < 8)
+        p[i] = 0;
+      else if (h < 12)
+        p[i] = uint8_t(c * 37);
+      else if (h < 14)
+        p[i] = uint8_t(rnd() & 7);
+      else
+        p[i] = uint8_t(rnd());
+    }
+  }
+}
+
+int main(int argc, char** argv)
+{
+  if (argc < 6) {
+    std::fprintf(stderr, "usage: codec_emu codec chunk_bytes n_chunks pattern seed\n");
+    return 2;
+  }
+  const std::string codec = argv[1];
+  const uint32_t chunk = uint32_t(std::stoul(argv[2]));
+  const uint64_t n = std::stoull(argv[3]);
+  const std::string pat = argv[4];
+  rng_state = std::stoull(argv[5]);
+  const uint64_t in_stride = (chunk + 255) / 256 * 256;
+  const uint64_t bound = codec == "zstd"
+                           ? chunk + (chunk >> 8) + (chunk < (128u << 10) ? ((128u << 10) - chunk) >> 11 : 0)
+                           : chunk + chunk / 255 + 16;
+  const uint64_t out_stride = (bound + 15) / 16 * 16;
+  std::vector<uint8_t> in(n * in_stride + 256), out(n * out_stride + 64);
+  std::vector<uint64_t> sizes(n);
+  std::vector<uint8_t> flat(n * chunk);
+  fill(flat.data(), flat.size(), pat, chunk);
+  for (uint64_t c = 0; c < n; ++c)
+    std::memcpy(in.data() + c * in_stride, flat.data() + c * chunk, chunk);
+  CodecBatch b{};
+  b.in = in.data();
+  b.in_stride = in_stride;
+  b.chunk_bytes = chunk;
+  b.n_chunks = n;
+  b.out = out.data();
+  b.out_stride = out_stride;
+  b.out_sizes = sizes.data();
+  b.level = 1;
+  const size_t sb = codec == "zstd" ? zstd_scratch_bytes(n, chunk)
+                                    : lz4_scratch_bytes(n, chunk);
+  std::vector<uint8_t> scratch(sb);
+  const cudaError_t e = codec == "zstd" ? launch_zstd(b, scratch.data(), nullptr)
+                                        : launch_lz4(b, scratch.data(), nullptr);
+  if (e != cudaSuccess) {
+    std::fprintf(stderr, "launch failed %d\n", e);
+    return 1;
+  }
+  void* zl = dlopen("libzstd.so.1", RTLD_NOW);
+  void* ll = dlopen("liblz4.so.1", RTLD_NOW);
+  auto zd = (size_t(*)(void*, size_t, const void*, size_t))(zl ? dlsym(zl, "ZSTD_decompress") : nullptr);
+  auto ze = (unsigned (*)(size_t))(zl ? dlsym(zl, "ZSTD_isError") : nullptr);
+  auto zn = (const char* (*)(size_t))(zl ? dlsym(zl, "ZSTD_getErrorName") : nullptr);
+  auto ld = (int (*)(const char*, char*, int, int))(ll ? dlsym(ll, "LZ4_decompress_safe") : nullptr);
+  if (!zd || !ld) {
+    std::fprintf(stderr, "stock codecs missing\n");
+    return 3;
+  }
+  uint64_t comp = 0;
+  std::vector<uint8_t> dec(chunk + 64);
+  for (uint64_t c = 0; c < n; ++c) {
+    const uint8_t* src = out.data() + c * out_stride;
+    if (sizes[c] > bound) {
+      std::fprintf(stderr, "chunk %llu: size %llu above bound %llu\n",
+                   (unsigned long long)c, (unsigned long long)sizes[c],
+                   (unsigned long long)bound);
+      return 1;
+    }
+    size_t got;
+    if (codec == "zstd") {
+      got = zd(dec.data(), dec.size(), src, sizes[c]);
+      if (ze(got)) {
+        std::fprintf(stderr, "chunk %llu: zstd error %s\n", (unsigned long long)c, zn(got));
+        return 1;
+      }
+    } else {
+      const int r = ld((const char*)src, (char*)dec.data(), int(sizes[c]), int(chunk));
+      if (r < 0) {
+        std::fprintf(stderr, "chunk %llu: lz4 error %d\n", (unsigned long long)c, r);
+        return 1;
+      }
+      got = size_t(r);
+    }
+    if (got != chunk || std::memcmp(dec.data(), flat.data() + c * chunk, chunk)) {
+      size_t at = 0;
+      while (at < chunk && dec[at] == flat[c * chunk + at])
+        ++at;
+      std::fprintf(stderr, "chunk %llu: decoded bytes differ (got %zu, first at %zu: %u vs %u)\n",
+                   (unsigned long long)c, got, at, unsigned(dec[at]),
+                   unsigned(flat[c * chunk + at]));
+      return 1;
+    }
+    comp += sizes[c];
+  }
+  std::printf("ok %s chunk=%u n=%llu pattern=%s ratio=%.3f\n", codec.c_str(), chunk,
+              (unsigned long long)n, pat.c_str(), double(n * chunk) / double(comp));
+  return 0;
+}

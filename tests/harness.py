@@ -231,3 +231,72 @@ def diff_shards(a, b):
             else:
                 out.append(f"{k}: finalized {x[1]}/{y[1]}")
     return out
+
+
+class _Info(C.Structure):
+    _fields_ = [("nlod", C.c_int), ("append_downsample", C.c_int),
+                ("epochs_per_batch", C.c_uint32), ("total_chunks", C.c_uint64),
+                ("chunk_elements", C.c_uint64), ("epoch_elements", C.c_uint64),
+                ("max_output_size", C.c_uint64),
+                ("lod_nelem", C.c_uint64 * 32), ("level_chunks", C.c_uint64 * 32),
+                ("shard_inner_count", C.c_uint64 * 32),
+                ("chunks_per_shard_total", C.c_uint64 * 32),
+                ("chunks_per_shard_append", C.c_uint64 * 32),
+                ("fixed_dims_count", C.c_uint64)]
+
+
+def plan_info(cfg):
+    lib = oracle()
+    lib.oracle_stream_info.argtypes = [C.c_void_p, C.POINTER(_Info)]
+    sink = MemSink()
+    try:
+        s = lib.oracle_stream_create(C.byref(cfg), sink.base)
+        info = _Info()
+        lib.oracle_stream_info(s, C.byref(info))
+        lib.oracle_stream_destroy(s)
+        return info
+    finally:
+        sink.close()
+
+
+def decode(codec, blob, raw_size):
+    lib = oracle()
+    src = C.create_string_buffer(blob, len(blob))
+    dst = C.create_string_buffer(raw_size + 64)
+    if codec == "zstd":
+        n = lib.oracle_zstd_decompress(dst, raw_size + 64, src, len(blob))
+    else:
+        n = lib.oracle_lz4_decompress(dst, raw_size, src, len(blob))
+    if n == C.c_size_t(-1).value:
+        raise ValueError(f"{codec} decode failed")
+    return dst.raw[:n]
+
+
+def compare_decoded(cfg_codec, shards_codec, shards_raw, codec):
+    """Decode every chunk of the compressed shards with the stock library and
+    compare with the raw chunk bytes of the CODEC_NONE shards.  Returns
+    (number of chunks checked, compressed bytes, raw bytes)."""
+    info = plan_info(cfg_codec)
+    chunk_bytes = info.chunk_elements * {1: 1}.get(0, 1)
+    assert set(shards_codec) == set(shards_raw), (sorted(shards_codec), sorted(shards_raw))
+    checked = comp_total = raw_total = 0
+    for key, (blob, fin) in shards_codec.items():
+        raw_blob, raw_fin = shards_raw[key]
+        assert fin and raw_fin
+        nslots = info.chunks_per_shard_total[key[0]]
+        idx_c, ok_c = parse_shard(blob, nslots)
+        idx_r, ok_r = parse_shard(raw_blob, nslots)
+        assert ok_c and ok_r, "index crc32c mismatch"
+        for (oc, nc), (orr, nr) in zip(idx_c.tolist(), idx_r.tolist()):
+            empty_c = oc == 0xFFFFFFFFFFFFFFFF and nc == 0xFFFFFFFFFFFFFFFF
+            empty_r = orr == 0xFFFFFFFFFFFFFFFF and nr == 0xFFFFFFFFFFFFFFFF
+            assert empty_c == empty_r
+            if empty_c:
+                continue
+            raw = raw_blob[orr:orr + nr]
+            got = decode(codec, blob[oc:oc + nc], len(raw))
+            assert got == raw, f"chunk mismatch in shard {key}"
+            checked += 1
+            comp_total += nc
+            raw_total += nr
+    return checked, comp_total, raw_total
