@@ -1,0 +1,355 @@
+"""Pipeline ingest benchmark (one JSON line on stdout).
+
+Workload (the plain multiscale configuration): two 256^3 arrays streamed
+through the GPU writer back to back --
+  * u16, v = ((x ^ y ^ z) * 257 + U{0..15}) mod 65536, LOD mean;
+  * f32, v = sin(0.05 x) cos(0.07 y) z / 256 + N(0, 0.01), LOD median;
+z, y, x = 256, chunk 64^3, shard 4x4x4 chunks, 2x2x2 pyramid (z folded across
+epochs, dim-0 method mean; the level rule gives 3 levels), zstd level 3,
+discard sink.  Inputs are seeded synthetic data.
+
+One step = restart both streams (device buffers are kept), append each whole
+cube, flush (every shard delivered to the sink).
+  value : inputs already resident in HBM (device pointers to append)
+  e2e   : the same from pinned host buffers (H2D inside the timed region)
+Both are GB/s of input bytes.  L2 is flushed (a 256 MiB write) between steps.
+
+--impl reference times the CPU oracle of the same path (the reference's CPU
+algorithm restated in oracle/, zstd from the system libzstd) on all host
+cores, on a bounded sample of the workload (the u16 cube).
+
+Under torchrun (N > 1) every rank runs an independent replica ("replicas
+only": the path has no exchange step); value = all ranks' bytes / max time.
+"""
+import argparse
+import ctypes as C
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np
+
+from chucky_gb300 import capi
+
+SIDE = 256
+CHUNK = 64
+METRIC = "pipeline ingest GB/s"
+
+
+def make_cubes(seed=7):
+    rng = np.random.default_rng(seed)
+    z, y, x = np.meshgrid(np.arange(SIDE), np.arange(SIDE), np.arange(SIDE),
+                          indexing="ij")
+    u16 = (((x ^ y ^ z) * 257 + rng.integers(0, 16, size=x.shape)) % 65536).astype("<u2")
+    f32 = (np.sin(0.05 * x) * np.cos(0.07 * y) * z / 256.0
+           + rng.normal(0, 0.01, size=x.shape)).astype("<f4")
+    return u16, f32
+
+
+def make_config(dtype, reduce):
+    dims = capi.make_dims([dict(size=SIDE, chunk=CHUNK, cps=4, downsample=1, name=n)
+                           for n in "zyx"])
+    cfg = capi.make_config(dims, dtype=dtype, codec="zstd", level=3, reduce=reduce,
+                           append_reduce="mean", max_nlod=4,
+                           buffer_capacity_bytes=128 << 20)
+    cfg._dims = dims
+    return cfg
+
+
+WORKLOAD = ("256^3 u16 (mean LOD) + 256^3 f32 (median LOD), chunk 64^3, shard "
+            "4^3 chunks, 2x2x2 pyramid (3 levels), zstd-3, discard sink")
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+
+    def __init__(self):
+        self.samples = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi",
+                 "--query-gpu=clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,"
+                 "clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "100", "-i",
+                 os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0] or "0"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 6:
+                self.samples.append(parts)
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                pass
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                 "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4)
+                          if s[2 + i].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.samples)}
+
+
+def run_ours(args, rank, world):
+    import torch
+    import chucky_gb300 as cg
+    from chucky_gb300 import build as cgbuild
+
+    cgbuild.build()
+    lib = cg.load()
+    lib.chucky_discard_sink_create.restype = C.c_void_p
+    lib.chucky_discard_sink_bytes.restype = C.c_uint64
+    lib.chucky_discard_sink_bytes.argtypes = [C.c_void_p]
+    lib.chucky_discard_sink_destroy.argtypes = [C.c_void_p]
+    lib.tile_stream_gpu_restart.argtypes = [C.c_void_p, C.c_void_p]
+    lib.chucky_launch_count.restype = C.c_uint64
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    torch.cuda.set_device(dev)
+
+    u16, f32 = make_cubes()
+    host = [torch.from_numpy(a.reshape(-1).view(np.uint8)).pin_memory() for a in (u16, f32)]
+    devbuf = [h.to(dev) for h in host]
+    nbytes = sum(h.numel() for h in host)
+    sink = lib.chucky_discard_sink_create()
+    cfgs = [make_config("u16", "mean"), make_config("f32", "median")]
+    streams = [cg.GpuStream(c, sink) for c in cfgs]
+    flush_buf = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+
+    def step(bufs):
+        for s, b in zip(streams, bufs):
+            if lib.tile_stream_gpu_restart(s.h, None) != 0:
+                raise RuntimeError("restart failed")
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        t0.record()
+        for s, b in zip(streams, bufs):
+            r = s.append(b.data_ptr(), b.numel())
+            if r.error:
+                raise RuntimeError(f"append failed {r.error}")
+        for s in streams:
+            r = s.flush()
+            if r.error:
+                raise RuntimeError(f"flush failed {r.error}")
+        t1.record()
+        torch.cuda.synchronize()
+        return t0.elapsed_time(t1)
+
+    def timed(bufs, k, w):
+        for _ in range(w):
+            step(bufs)
+        base_metrics = [s.metrics() for s in streams]
+        base_sink = lib.chucky_discard_sink_bytes(sink)
+        base_launch = lib.chucky_launch_count()
+        times = []
+        for _ in range(k):
+            flush_buf.fill_(1)  # evict L2 between steps
+            times.append(step(bufs))
+        end_metrics = [s.metrics() for s in streams]
+        sink_b = (lib.chucky_discard_sink_bytes(sink) - base_sink) / k
+        launches = lib.chucky_launch_count() - base_launch
+        return times, base_metrics, end_metrics, sink_b, launches
+
+    clocks = Clocks()
+    if rank == 0:
+        clocks.start()
+    times_dev, m0, m1, sink_b, launches = timed(devbuf, args.steps, args.warmup)
+    times_host, _, _, sink_h, launches_h = timed(host, args.steps, max(1, args.warmup // 2))
+    clk = clocks.stop() if rank == 0 else None
+
+    ms_dev = float(np.sum(times_dev))
+    ms_host = float(np.sum(times_host))
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms_dev, ms_host], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_dev, ms_host = float(t[0]), float(t[1])
+    total = nbytes * args.steps * world
+    value = total / (ms_dev * 1e-3) / 1e9
+    e2e = total / (ms_host * 1e-3) / 1e9
+
+    # dominant kernel: the zstd encoder (find + block + frame launches),
+    # event-timed on its own stream inside the library
+    comp_ms = sum(b.compress.ms - a.compress.ms for a, b in zip(m0, m1))
+    comp_in = sum(b.compress.input_bytes - a.compress.input_bytes for a, b in zip(m0, m1))
+    comp_launches = sum(b.compress.count - a.compress.count for a, b in zip(m0, m1))
+    per_launch_ms = comp_ms / max(1, comp_launches)
+    per_launch_bytes = comp_in / max(1, comp_launches)
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    peak, peak_src = 6800.0, "fallback"
+    if os.path.exists(peaks_path):
+        peak = float(json.load(open(peaks_path))["hbm_gbs"])
+        peak_src = "measured"
+    # algorithmic bytes of one encoder launch: chunk bytes read + compressed
+    # bytes written (the compressed bytes are what the sink receives)
+    launches_per_step = comp_launches / args.steps
+    out_per_launch = sink_b / max(1.0, launches_per_step)
+    achieved = ((per_launch_bytes + out_per_launch) / (per_launch_ms * 1e-3) / 1e9
+                if per_launch_ms > 0 else 0.0)
+    stages = {}
+    for name in capi.METRIC_NAMES:
+        ms = sum(getattr(b, name).ms - getattr(a, name).ms for a, b in zip(m0, m1))
+        if ms > 0:
+            stages[name] = round(ms / args.steps, 4)
+
+    for s in streams:
+        s.close()
+    lib.chucky_discard_sink_destroy(sink)
+    if rank != 0:
+        return None
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": "GB/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(ms_dev / args.steps, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u16+f32",
+        "data": "synthetic (seeded xor+noise u16 cube, sin*cos f32 cube + N(0,0.01))",
+        "config": {"workload": WORKLOAD, "input_bytes_per_step": nbytes,
+                   "l2": "flushed between steps (256 MiB write)",
+                   "parallelism": f"replicas x{world}",
+                   "stage_ms_per_step": stages},
+        "e2e": {"value": round(e2e, 3), "unit": "GB/s",
+                "h2d_bytes_per_step": nbytes,
+                "d2h_bytes_per_step": int(sink_h),
+                "ms_per_step": round(ms_host / args.steps, 4)},
+        # delivered chunk bytes (every pyramid level) / compressed shard bytes
+        "compression_ratio": round(comp_in / args.steps / max(1.0, sink_b), 4),
+        "roofline": {"kernel": "zstd encoder (find+block+frame)", "bound": "hbm",
+                     "achieved": round(achieved, 2), "peak": peak,
+                     "unit": "GB/s", "frac": round(achieved / peak, 4),
+                     "peak_source": peak_src, "traffic": None,
+                     "input_gbs": round(per_launch_bytes / (per_launch_ms * 1e-3) / 1e9, 2)
+                     if per_launch_ms > 0 else None},
+        "gpu_launches": int(launches),
+        "clocks": clk,
+    }
+    if args.cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(args)
+    return line
+
+
+def cpu_oracle_step(cube, cfg, threads):
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import harness as H
+    lib = H.oracle()
+    sink = lib.oracle_null_sink_create()
+    cfg.max_threads = threads
+    s = lib.oracle_stream_create(C.byref(cfg), sink)
+    if not s:
+        raise RuntimeError("oracle stream create failed")
+    buf = np.ascontiguousarray(cube).view(np.uint8).reshape(-1)
+    t0 = time.perf_counter()
+    w = lib.oracle_stream_writer(s).contents
+    wp = lib.oracle_stream_writer(s)
+    r = w.append(wp, capi.Slice(buf.ctypes.data, buf.ctypes.data + buf.size))
+    if r.error:
+        raise RuntimeError("oracle append failed")
+    r = w.flush(wp)
+    dt = time.perf_counter() - t0
+    out = lib.oracle_null_sink_bytes(sink)
+    lib.oracle_stream_destroy(s)
+    lib.oracle_null_sink_destroy(sink)
+    return dt, buf.size, out
+
+
+def cpu_baseline(args):
+    """The oracle on all host cores, whole workload, repeated for ~10 s."""
+    threads = os.cpu_count() or 1
+    u16, f32 = make_cubes()
+    work = [(u16, make_config("u16", "mean")), (f32, make_config("f32", "median"))]
+    tot_t, tot_b, passes = 0.0, 0, 0
+    while passes < 30 and (passes < 1 or tot_t < 10.0):
+        for cube, cfg in work:
+            dt, nb, _ = cpu_oracle_step(cube, cfg, threads)
+            tot_t += dt
+            tot_b += nb
+        passes += 1
+    return {"value": round(tot_b / tot_t / 1e9, 4), "unit": "GB/s", "cores": threads,
+            "kind": "port",
+            "sample": f"{passes} passes over the whole workload (both 256^3 cubes, "
+                      f"{tot_t:.1f} s of CPU time) through the oracle/ restatement of "
+                      "the reference CPU backend, zstd-3 from the system libzstd"}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return None
+    threads = os.cpu_count() or 1
+    u16, _ = make_cubes()
+    cfg = make_config("u16", "mean")
+    for _ in range(args.warmup):
+        cpu_oracle_step(u16, cfg, threads)
+    tot_t, tot_b = 0.0, 0
+    for _ in range(args.steps):
+        dt, nb, _ = cpu_oracle_step(u16, cfg, threads)
+        tot_t += dt
+        tot_b += nb
+    v = tot_b / tot_t / 1e9
+    return {"impl": "reference", "metric": METRIC, "value": round(v, 4), "unit": "GB/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(tot_t / args.steps * 1e3, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "u16", "data": "synthetic",
+            "config": {"workload": WORKLOAD,
+                       "sample": "u16 cube only (the CPU path, bounded)"},
+            "cpu_baseline": {"value": round(v, 4), "unit": "GB/s", "cores": threads,
+                             "kind": "port",
+                             "sample": "256^3 u16 cube per step through the oracle/ "
+                                       "restatement of the reference CPU backend"},
+            "e2e": {"value": round(v, 4), "unit": "GB/s",
+                    "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+        dist.init_process_group("nccl")
+    if args.impl == "reference":
+        line = run_reference(args, rank, world)
+    else:
+        line = run_ours(args, rank, world)
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+        dist.destroy_process_group()
+    if rank == 0 and line is not None:
+        print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

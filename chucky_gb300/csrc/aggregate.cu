@@ -9,9 +9,10 @@
 //      absorbs the padding that rounds the group to the shard alignment;
 //   4. exclusive scan -> byte offsets (offsets[positions] = total);
 //   5. every chunk's bytes are copied to out + offsets[perm[i]].
-// Steps 1-4 run in one CTA per level (a few thousand positions); step 5 is a
-// warp per chunk with aligned 32-bit stores built by funnel shifts, so the
-// byte-granular destination never needs unaligned accesses.
+// Steps 1-4 run in one CTA per level (a few thousand positions); step 5
+// spreads 16 KiB pieces of every chunk over the grid (a warp per piece,
+// aligned 16-byte stores assembled by funnel shifts, copy.cuh).
+#include "copy.cuh"
 #include "kernels.hpp"
 
 namespace chucky {
@@ -92,38 +93,21 @@ agg_layout_k(AggBatch b, uint64_t* scratch, uint64_t scratch_stride)
     L.offsets[L.positions] = carry;
 }
 
-// Copy `n` bytes from 4-byte aligned `src` to byte address `dst` with one
-// warp.  Full destination words are assembled from two aligned source words.
-__device__ void warp_copy(uint8_t* dst, const uint8_t* src, uint64_t n)
-{
-  const int lane = threadIdx.x & 31;
-  const uint64_t lead = (4 - (uintptr_t(dst) & 3)) & 3;
-  const uint64_t head = n < lead ? n : lead;
-  if (lane < head)
-    dst[lane] = src[lane];
-  const uint64_t body = (n - head) & ~uint64_t(3);
-  uint32_t* d = reinterpret_cast<uint32_t*>(dst + head);
-  const uint32_t* s = reinterpret_cast<const uint32_t*>(src);
-  const unsigned sh = unsigned(head) * 8; // source starts `head` bytes in
-  for (uint64_t w = lane; w < body / 4; w += 32) {
-    if (sh == 0)
-      d[w] = s[w];
-    else
-      d[w] = __funnelshift_r(s[w], s[w + 1], sh);
-  }
-  const uint64_t done = head + body;
-  if (lane < n - done)
-    dst[done + lane] = src[done + lane];
-}
+// One warp per 16 KiB piece of one chunk: (chunk, piece) pairs are spread
+// over the grid so that a few large chunks still keep every SM busy; the
+// copy itself uses aligned 16-byte stores (copy.cuh).
+constexpr uint64_t kPiece = 16 << 10;
 
 __global__ void __launch_bounds__(128)
-agg_gather_k(AggBatch b, uint64_t total_warps)
+agg_gather_k(AggBatch b, uint64_t total_chunks, uint64_t pieces_per_chunk)
 {
   const uint64_t warp = (blockIdx.x * uint64_t(blockDim.x) + threadIdx.x) >> 5;
   const uint64_t nwarps = (uint64_t(gridDim.x) * blockDim.x) >> 5;
-  for (uint64_t w = warp; w < total_warps; w += nwarps) {
+  const unsigned lane = threadIdx.x & 31;
+  for (uint64_t w = warp; w < total_chunks * pieces_per_chunk; w += nwarps) {
+    uint64_t i = w / pieces_per_chunk;
+    const uint64_t piece = w - i * pieces_per_chunk;
     int l = 0;
-    uint64_t i = w;
     while (l < b.nlevels && i >= b.lv[l].n) {
       i -= b.lv[l].n;
       ++l;
@@ -133,9 +117,12 @@ agg_gather_k(AggBatch b, uint64_t total_warps)
     const AggLevel& L = b.lv[l];
     const uint32_t c = L.gather[i];
     const uint64_t n = b.sizes[c];
-    if (n == 0)
+    const uint64_t off = piece * kPiece;
+    if (off >= n)
       continue;
-    warp_copy(L.out + L.offsets[L.perm[i]], b.comp + c * b.comp_stride, n);
+    const uint64_t len = n - off < kPiece ? n - off : kPiece;
+    copy_bytes(L.out + L.offsets[L.perm[i]] + off,
+               b.comp + c * b.comp_stride + off, len, lane, 32);
   }
 }
 
@@ -160,10 +147,13 @@ cudaError_t launch_aggregate(const AggBatch& b,
     total += b.lv[l].n;
   }
   agg_layout_k<<<b.nlevels, kScanThreads, 0, st>>>(b, scratch, stride);
+  note_launches(1);
   if (total) {
-    const uint64_t blocks = (total + 3) / 4;
-    const int grid = int(blocks < 152 * 32 ? blocks : 152 * 32);
-    agg_gather_k<<<grid, 128, 0, st>>>(b, total);
+    const uint64_t ppc = (b.comp_stride + kPiece - 1) / kPiece;
+    const uint64_t blocks = (total * ppc + 3) / 4;
+    const int grid = int(blocks < 152 * 64 ? blocks : 152 * 64);
+    agg_gather_k<<<grid, 128, 0, st>>>(b, total, ppc);
+    note_launches(1);
   }
   return cudaGetLastError();
 }
@@ -174,6 +164,7 @@ cudaError_t launch_fill_u64(uint64_t* p, uint64_t v, uint64_t n, cudaStream_t st
     return cudaSuccess;
   const uint64_t blocks = (n + 255) / 256;
   fill_u64_k<<<int(blocks < 1024 ? blocks : 1024), 256, 0, st>>>(p, v, n);
+  note_launches(1);
   return cudaGetLastError();
 }
 

@@ -3,6 +3,7 @@
 #include "plan.hpp"
 #include "stream.gpu.h"
 
+#include <atomic>
 #include <chrono>
 #include <cstdio>
 #include <cstring>
@@ -412,4 +413,20 @@ tile_stream_gpu_advise_chunk_sizes(tile_stream_configuration* config,
       return 0;
   }
   return 1;
+}
+
+// ---- launch counter ---------------------------------------------------------
+
+namespace chucky {
+static std::atomic<uint64_t> g_launches{ 0 };
+void note_launches(unsigned n)
+{
+  g_launches += n;
+}
+} // namespace chucky
+
+extern "C" uint64_t
+chucky_launch_count(void)
+{
+  return chucky::g_launches.load();
 }

@@ -26,10 +26,14 @@ int Stream::codec_init()
   }
   if (P.chunk_bytes >= (uint64_t(1) << 32))
     return 1;
+  for (int i = 0; i < 2; ++i)
+    if (cudaMallocHost(&h_chunk_ids[i], n * 4) != cudaSuccess ||
+        cudaMalloc(&d_chunk_ids[i], n * 4) != cudaSuccess)
+      return 1;
   return cudaMalloc(&codec_state, bytes) == cudaSuccess ? 0 : 1;
 }
 
-int Stream::codec_compress(uint64_t nchunks)
+int Stream::codec_compress(uint64_t nchunks, const uint32_t* d_ids)
 {
   CodecBatch b{};
   b.in = d_pool;
@@ -40,6 +44,7 @@ int Stream::codec_compress(uint64_t nchunks)
   b.out_stride = comp_stride;
   b.out_sizes = d_sizes;
   b.level = cfg.codec.level;
+  b.chunk_ids = d_ids;
   cudaError_t e = cudaErrorInvalidValue;
   if (cfg.codec.id == CODEC_LZ4_NON_STANDARD)
     e = launch_lz4(b, codec_state, s_comp);
@@ -58,6 +63,12 @@ void Stream::codec_release()
 {
   cudaFree(codec_state);
   codec_state = nullptr;
+  for (int i = 0; i < 2; ++i) {
+    cudaFreeHost(h_chunk_ids[i]);
+    cudaFree(d_chunk_ids[i]);
+    h_chunk_ids[i] = nullptr;
+    d_chunk_ids[i] = nullptr;
+  }
 }
 
 } // namespace chucky

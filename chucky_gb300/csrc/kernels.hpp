@@ -2,6 +2,7 @@
 #pragma once
 
 #include "common.cuh"
+#include "kernels_codec.hpp"
 #include "dtype.h"
 #include "types.lod.h"
 
@@ -72,6 +73,38 @@ cudaError_t launch_lod_to_chunks(const LodMortonArgs& a,
                                  const uint8_t* values,
                                  uint8_t* slot,
                                  cudaStream_t st);
+
+// Tiled single-pass pyramid (1..3 LOD dims, nlod - 1 <= lod_tile_levels).
+struct LodTileArgs
+{
+  int dtype, method, append_method, nlod, lod_ndim;
+  uint64_t fixed_count;
+  const uint8_t* linear; // row-major epoch buffer
+  uint8_t* slot;         // epoch slot of the chunk pool
+  uint8_t* accum;        // dense dim-0 accumulators, levels >= 1
+  uint32_t emit_mask;    // levels stored into the slot this epoch
+  uint32_t fold_mask;    // levels folded into the accumulators
+  uint32_t count[16];    // folds so far per level (before this epoch)
+  uint64_t tiles[3];     // L0 tiles per LOD dim
+  int64_t in_stride[3];  // epoch-buffer stride of each LOD dim
+  uint32_t cs[3];        // chunk extent of each LOD dim
+  const uint64_t* gather_fixed; // [fixed] epoch-buffer offset per slice
+  struct Level
+  {
+    uint64_t shape[3];             // LOD extents at this level
+    uint64_t S[3], s[3];           // chunk / within-chunk strides
+    const uint64_t* chunk_fixed;   // [fixed] slot offset per slice
+    uint64_t accum_off;            // level start in the accumulators
+    uint64_t nelem;                // product of shape
+  } lv[16];
+};
+int lod_tile_levels(int lod_ndim);
+uint32_t lod_tile_edge(int lod_ndim);
+cudaError_t launch_lod_tile(const LodTileArgs& a, cudaStream_t st);
+cudaError_t launch_lod_drain(const LodTileArgs& a,
+                             int level,
+                             uint32_t count,
+                             cudaStream_t st);
 
 // ---- (d) aggregation --------------------------------------------------------
 

@@ -7,17 +7,27 @@
 
 namespace chucky {
 
+// Number of kernels this library has launched (process-wide).
+void note_launches(unsigned n);
+
 struct CodecBatch
 {
   const uint8_t* in;    // first chunk (4-byte aligned)
   uint64_t in_stride;   // bytes between chunks
   uint32_t chunk_bytes; // codec input per chunk
-  uint64_t n_chunks;
+  uint64_t n_chunks;     // chunks to encode (entries of chunk_ids if set)
   uint8_t* out;         // compressed slots
   uint64_t out_stride;  // bytes between slots (>= bound)
   uint64_t* out_sizes;  // [n_chunks] compressed sizes (written)
   uint32_t segs_per_chunk;
   int level;
+  const uint32_t* chunk_ids; // optional: encode only these chunk slots
+
+  // slot of the i-th chunk of the batch
+  __host__ __device__ uint64_t id(uint64_t i) const
+  {
+    return chunk_ids ? chunk_ids[i] : i;
+  }
 };
 
 size_t lz4_scratch_bytes(uint64_t n_chunks, uint32_t chunk_bytes);

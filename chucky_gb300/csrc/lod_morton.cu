@@ -15,159 +15,13 @@
 // mean (u8/u16 -> u32, u32 -> u64, i8/i16 -> i32, i32 -> i64, f16 -> f32),
 // insertion-sort median (upper median), second-extreme with >= / <= ties.
 #include "kernels.hpp"
+#include "lod_ops.cuh"
 
 namespace chucky {
 
 namespace lod {
 
 constexpr int kThreads = 256;
-
-template<typename T>
-__device__ __forceinline__ bool lt(T a, T b)
-{
-  return a < b;
-}
-template<>
-__device__ __forceinline__ bool lt<__half>(__half a, __half b)
-{
-  return __half2float(a) < __half2float(b);
-}
-
-template<typename T>
-__device__ __forceinline__ T from_acc(typename WideAcc<T>::type v)
-{
-  return T(v);
-}
-template<>
-__device__ __forceinline__ __half from_acc<__half>(float v)
-{
-  return __float2half_rn(v);
-}
-
-template<typename T>
-__device__ __forceinline__ typename WideAcc<T>::type to_acc(T v)
-{
-  return typename WideAcc<T>::type(v);
-}
-template<>
-__device__ __forceinline__ float to_acc<__half>(__half v)
-{
-  return __half2float(v);
-}
-
-// Reduce src[0..n) in order.
-template<typename T>
-__device__ T reduce_window(const T* src, uint64_t n, int method)
-{
-  using A = typename WideAcc<T>::type;
-  switch (method) {
-    case lod_reduce_mean: {
-      A sum = A(0);
-      for (uint64_t j = 0; j < n; ++j)
-        sum += to_acc<T>(src[j]);
-      return from_acc<T>(sum / A(n));
-    }
-    case lod_reduce_min: {
-      T v = src[0];
-      for (uint64_t j = 1; j < n; ++j)
-        if (lt(src[j], v))
-          v = src[j];
-      return v;
-    }
-    case lod_reduce_max: {
-      T v = src[0];
-      for (uint64_t j = 1; j < n; ++j)
-        if (lt(v, src[j]))
-          v = src[j];
-      return v;
-    }
-    case lod_reduce_median: {
-      T buf[16];
-      const uint64_t m = n <= 16 ? n : 16;
-      for (uint64_t j = 0; j < m; ++j)
-        buf[j] = src[j];
-      for (uint64_t i = 1; i < m; ++i) {
-        const T key = buf[i];
-        uint64_t k = i;
-        while (k > 0 && lt(key, buf[k - 1])) {
-          buf[k] = buf[k - 1];
-          --k;
-        }
-        buf[k] = key;
-      }
-      return buf[m / 2];
-    }
-    case lod_reduce_max_suppressed: {
-      T t1 = src[0], t2 = src[0];
-      for (uint64_t j = 1; j < n; ++j) {
-        const T v = src[j];
-        if (!lt(v, t1)) { // v >= t1
-          t2 = t1;
-          t1 = v;
-        } else if (lt(t2, v))
-          t2 = v;
-      }
-      return t2;
-    }
-    case lod_reduce_min_suppressed: {
-      T t1 = src[0], t2 = src[0];
-      for (uint64_t j = 1; j < n; ++j) {
-        const T v = src[j];
-        if (!lt(t1, v)) { // v <= t1
-          t2 = t1;
-          t1 = v;
-        } else if (lt(v, t2))
-          t2 = v;
-      }
-      return t2;
-    }
-  }
-  return src[0];
-}
-
-// (a + b) >> s without overflow for 8..32-bit integers; a + b otherwise
-// (the dim-0 mean divides at emit for floats; 64-bit ints just sum).
-template<typename T>
-__device__ __forceinline__ T add_shift(T a, T b, int s)
-{
-  if constexpr (IsFloat<T>::value || sizeof(T) >= 8) {
-    return T(a + b);
-  } else {
-    const T mask = T((1u << s) - 1);
-    return T((a >> s) + (b >> s) + (((a & mask) + (b & mask)) >> s));
-  }
-}
-template<>
-__device__ __forceinline__ __half add_shift<__half>(__half a, __half b, int)
-{
-  return __float2half_rn(__half2float(a) + __half2float(b));
-}
-
-template<typename T>
-__device__ __forceinline__ T fold_one(T acc, T v, int level, int method)
-{
-  if (method == lod_reduce_mean)
-    return add_shift<T>(acc, v, level);
-  if (method == lod_reduce_min)
-    return lt(v, acc) ? v : acc;
-  if (method == lod_reduce_max)
-    return lt(acc, v) ? v : acc;
-  return acc;
-}
-
-template<typename T>
-__device__ __forceinline__ T emit_one(T acc, uint32_t count, int method)
-{
-  if constexpr (IsFloat<T>::value) {
-    if (method == lod_reduce_mean) {
-      if constexpr (sizeof(T) == 2)
-        return __float2half_rn(__fdiv_rn(__half2float(acc), float(count)));
-      else
-        return T(acc / T(count));
-    }
-  }
-  return acc;
-}
 
 template<typename T>
 __global__ void __launch_bounds__(kThreads)
@@ -273,6 +127,7 @@ cudaError_t launch_lod_gather(const LodMortonArgs& a,
                           a.d_gather_fixed,
                           n0,
                           total)));
+  note_launches(1);
   return cudaGetLastError();
 }
 
@@ -292,6 +147,7 @@ cudaError_t launch_lod_reduce(const LodMortonArgs& a,
                             a.lod_nelem[l + 1],
                             total,
                             a.reduce_method)));
+    note_launches(1);
   }
   return cudaGetLastError();
 }
@@ -313,6 +169,7 @@ cudaError_t launch_lod_fold(const LodMortonArgs& a,
       count,
       level,
       a.append_method)));
+  note_launches(1);
   return cudaGetLastError();
 }
 
@@ -332,6 +189,7 @@ cudaError_t launch_lod_emit(const LodMortonArgs& a,
       n,
       count,
       a.append_method)));
+  note_launches(1);
   return cudaGetLastError();
 }
 
@@ -351,6 +209,7 @@ cudaError_t launch_lod_to_chunks(const LodMortonArgs& a,
       a.d_chunk_fixed[level],
       n,
       total)));
+  note_launches(1);
   return cudaGetLastError();
 }
 

@@ -55,7 +55,7 @@ lz4_find_k(CodecBatch b, Seq* seqs, SegMeta* meta)
     return;
   const uint64_t chunk = seg / b.segs_per_chunk;
   const uint32_t k = uint32_t(seg % b.segs_per_chunk);
-  const uint8_t* base = b.in + chunk * b.in_stride;
+  const uint8_t* base = b.in + b.id(chunk) * b.in_stride;
   const uint32_t n = b.chunk_bytes;
   const uint32_t s0 = k * kSegBytes;
   const uint32_t s1 = min(n, s0 + kSegBytes);
@@ -108,7 +108,7 @@ __global__ void lz4_plan_k(CodecBatch b, SegMeta* meta)
     }
   }
   off += lit_part(carry); // final literal-only sequence
-  b.out_sizes[chunk] = off;
+  b.out_sizes[b.id(chunk)] = off;
 }
 
 __device__ __forceinline__ uint8_t* put_len(uint8_t* o, uint32_t extra)
@@ -144,8 +144,8 @@ lz4_emit_k(CodecBatch b, const Seq* seqs, const SegMeta* meta)
   const bool last = k + 1 == b.segs_per_chunk;
   if (!m.nseq && !last)
     return; // its literals travel with the next segment
-  const uint8_t* in = b.in + chunk * b.in_stride;
-  uint8_t* out = b.out + chunk * b.out_stride;
+  const uint8_t* in = b.in + b.id(chunk) * b.in_stride;
+  uint8_t* out = b.out + b.id(chunk) * b.out_stride;
   const Seq* s = seqs + seg * kMaxSeqPerSeg;
   const uint32_t s0 = k * kSegBytes;
   uint64_t pos = m.out_off;
@@ -239,6 +239,7 @@ cudaError_t launch_lz4(CodecBatch b, void* scratch, cudaStream_t st)
   SegMeta* meta = reinterpret_cast<SegMeta*>((m + 255) & ~uintptr_t(255));
   const unsigned grid = unsigned((segs + kWarps - 1) / kWarps);
   cudaError_t e;
+  note_launches(3);
   CHUCKY_LAUNCH(lz4_find_k, grid, 32 * kWarps, 0, st, b, seqs, meta);
   if ((e = cudaGetLastError()) != cudaSuccess)
     return e;

@@ -301,6 +301,40 @@ int Stream::setup_lod()
     CK(cudaMemcpy(d_chunk_fixed[l], fixed.data(), P.fixed_count * 8,
                   cudaMemcpyHostToDevice));
   }
+  // The tiled kernel produces every level from one read of L0 when the
+  // LOD dims are 1..3 and the pyramid fits inside one tile.
+  if (P.lod_ndim >= 1 && P.lod_ndim <= 3 && P.nlod <= 16 &&
+      P.nlod - 1 <= lod_tile_levels(P.lod_ndim)) {
+    lod_tiled = true;
+    LodTileArgs& t = tile;
+    t.dtype = cfg.dtype;
+    t.method = cfg.reduce_method;
+    t.append_method = cfg.append_reduce_method;
+    t.nlod = P.nlod;
+    t.lod_ndim = P.lod_ndim;
+    t.fixed_count = P.fixed_count;
+    t.gather_fixed = d_gather_fixed;
+    const uint32_t edge = lod_tile_edge(P.lod_ndim);
+    for (int k = 0; k < P.lod_ndim; ++k) {
+      const int d = P.lod_to_dim[k];
+      t.tiles[k] = (P.lv[0].shape[d] + edge - 1) / edge;
+      t.in_stride[k] = int64_t(stride[d]);
+      t.cs[k] = uint32_t(cfg.dimensions[d].chunk_size);
+    }
+    for (int l = 0; l < nlod; ++l) {
+      const tile_stream_layout& L = P.lv[l].layout;
+      LodTileArgs::Level& V = t.lv[l];
+      V.nelem = P.lv[l].lod_nelem;
+      V.accum_off = accum_beg[l];
+      V.chunk_fixed = d_chunk_fixed[l];
+      for (int k = 0; k < P.lod_ndim; ++k) {
+        const int d = P.lod_to_dim[k];
+        V.shape[k] = P.lv[l].shape[d];
+        V.S[k] = uint64_t(L.lifted_strides[2 * d]);
+        V.s[k] = uint64_t(L.lifted_strides[2 * d + 1]);
+      }
+    }
+  }
   lod.dtype = cfg.dtype;
   lod.reduce_method = cfg.reduce_method;
   lod.append_method = cfg.append_reduce_method;
@@ -472,6 +506,34 @@ int Stream::run_epoch(uint64_t present)
     CK(launch_transpose(a, s_comp));
     if (timed_end(s_comp))
       return 1;
+  } else if (lod_tiled) {
+    const bool folding = P.append_downsample && d_accum;
+    LodTileArgs t = tile;
+    t.linear = d_epoch[b];
+    t.slot = slot_ptr;
+    t.accum = d_accum;
+    t.fold_mask = 0;
+    t.emit_mask = uint32_t((1ull << P.nlod) - 1);
+    mask = t.emit_mask;
+    if (folding) {
+      t.emit_mask = 1;
+      for (int l = 1; l < P.nlod; ++l) {
+        t.fold_mask |= 1u << l;
+        t.count[l] = counts[l];
+        if (counts[l] + 1 >= (1u << l))
+          t.emit_mask |= 1u << l;
+      }
+      mask = t.emit_mask;
+    }
+    if (timed_begin(s_comp, &metrics.lod_reduce, double(P.epoch_bytes),
+                    double(P.slot_bytes)))
+      return 1;
+    CK(launch_lod_tile(t, s_comp));
+    if (timed_end(s_comp))
+      return 1;
+    if (folding)
+      for (int l = 1; l < P.nlod; ++l)
+        counts[l] = (mask >> l & 1) ? 0 : counts[l] + 1;
   } else {
     const double vb = double(P.fixed_count * P.lv[0].lod_nelem * P.bpe);
     if (timed_begin(s_comp, &metrics.lod_gather, vb, vb))
@@ -532,10 +594,25 @@ int Stream::kick_batch(uint32_t n_epochs, const uint32_t* epoch_masks)
   const uint64_t nchunks = uint64_t(n_epochs) * P.total_chunks;
   const uint8_t* comp = d_pool;
   if (cfg.codec.id != CODEC_NONE) {
-    if (timed_begin(s_comp, &metrics.compress, double(nchunks * P.chunk_bytes),
-                    0))
+    // encode only the chunks of active (epoch, level) pairs
+    uint32_t* ids = h_chunk_ids[si];
+    uint64_t n = 0;
+    for (uint32_t e = 0; e < n_epochs; ++e)
+      for (int l = 0; l < P.nlod; ++l)
+        if (epoch_masks[e] >> l & 1) {
+          const uint64_t base = uint64_t(e) * P.total_chunks + P.lv[l].chunk_offset;
+          for (uint64_t j = 0; j < P.lv[l].layout.chunks_per_epoch; ++j)
+            ids[n++] = uint32_t(base + j);
+        }
+    const uint32_t* d_ids = nullptr;
+    if (n != nchunks) {
+      CK(cudaMemcpyAsync(d_chunk_ids[si], ids, n * 4, cudaMemcpyHostToDevice,
+                         s_comp));
+      d_ids = d_chunk_ids[si];
+    }
+    if (timed_begin(s_comp, &metrics.compress, double(n * P.chunk_bytes), 0))
       return 1;
-    if (codec_compress(nchunks))
+    if (codec_compress(n, d_ids))
       return 1;
     if (timed_end(s_comp))
       return 1;
@@ -804,9 +881,16 @@ int Stream::flush_all()
     uint32_t drain = 0;
     for (int l = 1; l < P.nlod; ++l)
       if (counts[l] > 0) {
-        CK(launch_lod_emit(lod, l, counts[l], d_accum, d_values, s_comp));
+        if (lod_tiled) {
+          LodTileArgs t = tile;
+          t.slot = pool_slot(0);
+          t.accum = d_accum;
+          CK(launch_lod_drain(t, l, counts[l], s_comp));
+        } else {
+          CK(launch_lod_emit(lod, l, counts[l], d_accum, d_values, s_comp));
+          CK(launch_lod_to_chunks(lod, l, d_values, pool_slot(0), s_comp));
+        }
         counts[l] = 0;
-        CK(launch_lod_to_chunks(lod, l, d_values, pool_slot(0), s_comp));
         drain |= 1u << l;
       }
     if (drain) {

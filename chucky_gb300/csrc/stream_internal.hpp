@@ -64,6 +64,8 @@ struct Stream
   uint64_t* d_sizes = nullptr;
   uint64_t comp_stride = 0;
   void* codec_state = nullptr;
+  uint32_t* h_chunk_ids[2] = {};   // pinned staging of the encode list
+  uint32_t* d_chunk_ids[2] = {};
 
   // transpose
   uint64_t* d_row_off = nullptr;
@@ -84,6 +86,8 @@ struct Stream
   uint64_t ends_beg[LOD_MAX_LEVELS] = {};
   uint32_t counts[LOD_MAX_LEVELS] = {};
   LodMortonArgs lod{};
+  bool lod_tiled = false; // single-pass tile kernel instead of Morton path
+  LodTileArgs tile{};
 
   // aggregation
   uint32_t* d_gather[LOD_MAX_LEVELS] = {};
@@ -143,7 +147,7 @@ struct Stream
   writer_result flush();
 
   int codec_init();
-  int codec_compress(uint64_t nchunks);
+  int codec_compress(uint64_t nchunks, const uint32_t* d_ids);
   void codec_release();
 
   int timed_begin(cudaStream_t st, stream_metric* m, double in, double out);

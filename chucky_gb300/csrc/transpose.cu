@@ -68,11 +68,13 @@ cudaError_t launch_transpose(const TransposeArgs& a, cudaStream_t st)
     const uint64_t nvec = a.n / per;
     if (nvec) {
       transpose_vec16_k<<<grid_for(nvec), kThreads, 0, st>>>(a, nvec);
+      note_launches(1);
       first = nvec * per;
     }
   }
   if (first < a.n) {
     const int g = grid_for(a.n - first);
+    note_launches(1);
     switch (a.bpe) {
       case 1:
         transpose_scalar_k<uint8_t><<<g, kThreads, 0, st>>>(a, first);

@@ -20,6 +20,7 @@
 // stream) -> frame (CTA per chunk: frame header + blocks).
 #include "kernels_codec.hpp"
 #include "launch.cuh"
+#include "copy.cuh"
 #include "lz77.cuh"
 
 namespace chucky {
@@ -223,7 +224,7 @@ zstd_find_k(CodecBatch b, Seq* seqs, ZSeg* meta)
     return;
   const uint64_t chunk = seg / b.segs_per_chunk;
   const uint32_t k = uint32_t(seg % b.segs_per_chunk);
-  const uint8_t* base = b.in + chunk * b.in_stride;
+  const uint8_t* base = b.in + b.id(chunk) * b.in_stride;
   const uint32_t s0 = k * kSegBytes;
   const uint32_t s1 = min(b.chunk_bytes, s0 + kSegBytes);
   Seq* out = seqs + seg * kMaxSeqPerSeg;
@@ -541,6 +542,7 @@ __device__ bool huff_describe(Huff& h)
 struct BlockShared
 {
   uint32_t hist[256];
+  uint32_t whist[kSegsPerBlock][256]; // per-warp histograms (merged)
   Huff huff;
   uint32_t seg_nseq[kSegsPerBlock];
   uint32_t seg_carry[kSegsPerBlock];
@@ -574,7 +576,7 @@ zstd_block_k(CodecBatch b,
   const uint64_t blk = blockIdx.x;
   const uint64_t chunk = blk / blocks_per_chunk;
   const uint32_t bi = uint32_t(blk % blocks_per_chunk);
-  const uint8_t* in = b.in + chunk * b.in_stride;
+  const uint8_t* in = b.in + b.id(chunk) * b.in_stride;
   const uint32_t b0 = bi * kBlockBytes;
   const uint32_t b1 = min(b.chunk_bytes, b0 + kBlockBytes);
   const uint32_t bsize = b1 - b0;
@@ -584,8 +586,8 @@ zstd_block_k(CodecBatch b,
   uint8_t* lits = lits_all + blk * kBlockBytes;
   uint8_t* stage = stage_all + blk * kStageBytes;
 
-  for (int i = tid; i < 256; i += blockDim.x)
-    S.hist[i] = 0;
+  for (int i = tid; i < 256 * int(kSegsPerBlock); i += blockDim.x)
+    (&S.whist[0][0])[i] = 0;
   if (tid == 0) {
     uint32_t carry = 0, matched_before = 0, nseq = 0;
     for (uint32_t k = 0; k < nsegs; ++k) {
@@ -606,9 +608,17 @@ zstd_block_k(CodecBatch b,
 
   // RLE block test
   {
+    // chunks are 16-byte aligned and blocks start at multiples of 128 KiB
     const uint8_t first = in[b0];
+    const uint32_t pat = first * 0x01010101u;
     bool same = true;
-    for (uint32_t i = tid; i < bsize && same; i += blockDim.x)
+    const uint32_t nv = bsize / 16;
+    const uint4* v = reinterpret_cast<const uint4*>(in + b0);
+    for (uint32_t i = tid; i < nv && same; i += blockDim.x) {
+      const uint4 q = v[i];
+      same = q.x == pat && q.y == pat && q.z == pat && q.w == pat;
+    }
+    for (uint32_t i = nv * 16 + tid; i < bsize && same; i += blockDim.x)
       same = in[b0 + i] == first;
     if (!same)
       S.all_same = 0;
@@ -656,7 +666,7 @@ zstd_block_k(CodecBatch b,
           for (uint32_t t = lane; t < n; t += 32) {
             const uint8_t c = in[src + si + t];
             lits[dst + di + t] = c;
-            atomicAdd(&S.hist[c], 1u);
+            atomicAdd(&S.whist[warp][c], 1u);
           }
         }
         src += tot_in;
@@ -667,10 +677,17 @@ zstd_block_k(CodecBatch b,
         for (uint32_t t = lane; t < n; t += 32) {
           const uint8_t c = in[src + t];
           lits[dst + t] = c;
-          atomicAdd(&S.hist[c], 1u);
+          atomicAdd(&S.whist[warp][c], 1u);
         }
       }
     }
+  }
+  __syncthreads();
+  for (int i = tid; i < 256; i += blockDim.x) {
+    uint32_t t = 0;
+    for (uint32_t w = 0; w < kSegsPerBlock; ++w)
+      t += S.whist[w][i];
+    S.hist[i] = t;
   }
   __syncthreads();
 
@@ -765,27 +782,48 @@ zstd_block_k(CodecBatch b,
     __syncthreads();
     if (S.lit_mode == 2) {
       uint8_t* sp = stage + S.stream_pos[st];
-      uint64_t pos = before;
-      // write codes; byte-wise atomicOr emulated on 32-bit words requires
-      // alignment, so OR bits into bytes with the owner-exclusive rule:
-      // boundary bytes go through 32-bit atomics on the containing word
+      // Bits of this thread: [before, before + bits) of the stream.  Whole
+      // 32-bit words inside that range belong to this thread alone and are
+      // stored plainly; the first and last (shared) words are OR-ed in.
       uint32_t* wbase = reinterpret_cast<uint32_t*>(
         reinterpret_cast<uintptr_t>(sp) & ~uintptr_t(3));
-      const uint32_t skew = uint32_t(reinterpret_cast<uintptr_t>(sp) & 3) * 8;
+      const uint64_t skew = uint64_t(reinterpret_cast<uintptr_t>(sp) & 3) * 8;
+      const uint64_t start = before + skew;
+      uint64_t word = start >> 5;
+      int fill = int(start & 31);
+      const bool first_shared = fill != 0;
+      bool first = true;
+      uint64_t acc = 0;
       for (uint32_t r = q0; r < q1; ++r) {
         const uint8_t c = lits[a1 - 1 - r];
-        const uint32_t L = S.huff.len[c];
-        const uint64_t p = pos + skew;
-        const uint64_t v = uint64_t(S.huff.code[c]) << (p & 31);
-        atomicOr(wbase + (p >> 5), uint32_t(v));
-        if ((p & 31) + L > 32)
-          atomicOr(wbase + (p >> 5) + 1, uint32_t(v >> 32));
-        pos += L;
+        acc |= uint64_t(S.huff.code[c]) << fill;
+        fill += S.huff.len[c];
+        if (fill >= 32) {
+          if (first && first_shared)
+            atomicOr(wbase + word, uint32_t(acc));
+          else
+            wbase[word] = uint32_t(acc);
+          first = false;
+          acc >>= 32;
+          fill -= 32;
+          ++word;
+        }
       }
-      if (t == 63) { // end mark
-        const uint64_t p = pos + skew;
-        atomicOr(wbase + (p >> 5), 1u << (p & 31));
+      if (t == 63) { // end mark after the stream's last bit
+        acc |= uint64_t(1) << fill;
+        fill += 1;
+        if (fill >= 32) {
+          if (first && first_shared)
+            atomicOr(wbase + word, uint32_t(acc));
+          else
+            wbase[word] = uint32_t(acc);
+          acc >>= 32;
+          fill -= 32;
+          ++word;
+        }
       }
+      if (fill > 0)
+        atomicOr(wbase + word, uint32_t(acc));
     }
   } else if (tid == 0 && nlit > 0 && S.lit_mode == 0) {
     // nothing to lay out yet (raw literals below)
@@ -914,9 +952,8 @@ zstd_frame_k(CodecBatch b,
              uint32_t blocks_per_chunk)
 {
   __shared__ uint32_t offs[1024];
-  __shared__ uint32_t hdr_len;
   const uint64_t chunk = blockIdx.x;
-  uint8_t* out = b.out + chunk * b.out_stride;
+  uint8_t* out = b.out + b.id(chunk) * b.out_stride;
   const uint32_t n = b.chunk_bytes;
   if (threadIdx.x == 0) {
     // magic, descriptor (single segment), frame content size
@@ -935,22 +972,18 @@ zstd_frame_k(CodecBatch b,
       put_le(out + 5, n, 4);
       h = 9;
     }
-    hdr_len = h;
     uint32_t acc = h;
     for (uint32_t k = 0; k < blocks_per_chunk && k < 1024; ++k) {
       offs[k] = acc;
       acc += block_sizes[chunk * blocks_per_chunk + k];
     }
-    b.out_sizes[chunk] = acc;
+    b.out_sizes[b.id(chunk)] = acc;
   }
   __syncthreads();
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  for (uint32_t k = warp; k < blocks_per_chunk; k += blockDim.x / 32) {
+  for (uint32_t k = 0; k < blocks_per_chunk; ++k) {
     const uint8_t* src = stage_all + (chunk * blocks_per_chunk + k) * kStageBytes;
     const uint32_t sz = block_sizes[chunk * blocks_per_chunk + k];
-    uint8_t* dst = out + offs[k];
-    for (uint32_t i = lane; i < sz; i += 32)
-      dst[i] = src[i];
+    copy_bytes(out + offs[k], src, sz, threadIdx.x, blockDim.x);
   }
 }
 
@@ -987,6 +1020,7 @@ cudaError_t launch_zstd(CodecBatch b, void* scratch, cudaStream_t st)
   p += blocks * kStageBytes;
   uint32_t* bsizes = reinterpret_cast<uint32_t*>(p);
   cudaError_t e;
+  note_launches(3);
   CHUCKY_LAUNCH(zstd_find_k, unsigned((segs + kFindWarps - 1) / kFindWarps), 32 * kFindWarps, 0, st, b, seqs, meta);
   if ((e = cudaGetLastError()) != cudaSuccess)
     return e;

@@ -29,6 +29,9 @@ extern "C"
   void chucky_discard_sink_destroy(struct shard_sink* s);
   uint64_t chucky_discard_sink_bytes(const struct shard_sink* s);
 
+  /* Number of CUDA kernels this library has launched in this process. */
+  uint64_t chucky_launch_count(void);
+
   /* crc32c (Castagnoli) of a buffer, as used by shard indexes. */
   uint32_t chucky_crc32c(const void* data, size_t len);
 

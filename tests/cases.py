@@ -51,6 +51,13 @@ CASES = [
      dict(reduce="mean"), 5),
     ("partial_epoch", [D(size=7, chunk=2, cps=2), D(size=8, chunk=4, cps=1),
                        D(size=16, chunk=8, cps=2)], dict(epochs_per_batch=2), 3.5),
+    ("lod4d_morton", [D(size=0, chunk=1, cps=2), D(size=6, chunk=2, cps=2, downsample=1),
+                      D(size=5, chunk=2, cps=0, downsample=1),
+                      D(size=4, chunk=2, cps=2, downsample=1),
+                      D(size=8, chunk=4, cps=1, downsample=1)],
+     dict(reduce="median"), 3),
+    ("deep1d_morton", [D(size=0, chunk=1, cps=2, downsample=1), D(size=4100, chunk=2, cps=64, downsample=1)],
+     dict(reduce="mean", append_reduce="max"), 5),
     ("aligned_shards", [D(size=8, chunk=2, cps=2), D(size=16, chunk=8, cps=1),
                         D(size=16, chunk=8, cps=2)], dict(shard_alignment=512), 4),
 ]

@@ -14,6 +14,10 @@
 
 using namespace chucky;
 
+namespace chucky {
+void note_launches(unsigned) {}
+} // namespace chucky
+
 static uint64_t rng_state;
 static uint64_t rnd()
 {
@@ -25,6 +29,20 @@ static uint64_t rnd()
 
 static void fill(uint8_t* p, size_t n, const std::string& pat, size_t chunk)
 {
+  if (pat.rfind("file:", 0) == 0) { // repeat the file's bytes
+    FILE* f = std::fopen(pat.c_str() + 5, "rb");
+    std::vector<uint8_t> d;
+    if (f) {
+      uint8_t buf[65536];
+      size_t k;
+      while ((k = std::fread(buf, 1, sizeof buf, f)) > 0)
+        d.insert(d.end(), buf, buf + k);
+      std::fclose(f);
+    }
+    for (size_t i = 0; i < n; ++i)
+      p[i] = d.empty() ? 0 : d[i % d.size()];
+    return;
+  }
   for (size_t i = 0; i < n; ++i) {
     if (pat == "zeros")
       p[i] = 0;
