@@ -56,14 +56,15 @@ def make_config(dtype, reduce):
     dims = capi.make_dims([dict(size=SIDE, chunk=CHUNK, cps=4, downsample=1, name=n)
                            for n in "zyx"])
     cfg = capi.make_config(dims, dtype=dtype, codec="zstd", level=3, reduce=reduce,
-                           append_reduce="mean", max_nlod=4,
+                           append_reduce="mean", max_nlod=4, epochs_per_batch=4,
                            buffer_capacity_bytes=128 << 20)
     cfg._dims = dims
     return cfg
 
 
 WORKLOAD = ("256^3 u16 (mean LOD) + 256^3 f32 (median LOD), chunk 64^3, shard "
-            "4^3 chunks, 2x2x2 pyramid (3 levels), zstd-3, discard sink")
+            "4^3 chunks, 2x2x2 pyramid (3 levels), zstd-3, K=4 epochs per batch "
+            "(one batch per array), discard sink")
 
 
 class Clocks:

@@ -12,6 +12,7 @@
 //          segment's first sequence and place every segment in the output
 //   emit : a warp writes its segment's sequences at that place.
 #include "kernels_codec.hpp"
+#include "copy.cuh"
 #include "launch.cuh"
 #include "lz77.cuh"
 
@@ -43,6 +44,9 @@ struct SegMeta
   uint32_t body;      // bytes of all sequences except sequence 0's literals
   uint32_t carry_in;  // literals carried in from earlier segments
   uint64_t out_off;   // byte offset of this segment's output in the chunk
+  uint64_t tail_dst;  // output offset of this segment's trailing literals
+  uint64_t final_off; // last segment: offset of the literal-only sequence
+  uint32_t final_ll;  // last segment: its literal count
 };
 
 __global__ void __launch_bounds__(32 * kWarps)
@@ -89,6 +93,10 @@ lz4_find_k(CodecBatch b, Seq* seqs, SegMeta* meta)
   }
 }
 
+// Place every segment's sequences, and every trailing literal run, in the
+// chunk's output.  Trailing literals of a segment (all of it when it has no
+// match) belong to the literal field of the next sequence: the first
+// sequence of a later segment, or the final literal-only sequence.
 __global__ void lz4_plan_k(CodecBatch b, SegMeta* meta)
 {
   const uint64_t chunk = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
@@ -96,18 +104,34 @@ __global__ void lz4_plan_k(CodecBatch b, SegMeta* meta)
     return;
   SegMeta* m = meta + chunk * b.segs_per_chunk;
   uint64_t off = 0;
-  uint32_t carry = 0;
+  uint32_t carry = 0;   // literals of the pending run
+  uint32_t run_first = 0; // first segment contributing to the pending run
+  auto settle = [&](uint64_t field, uint32_t upto) {
+    // the run's literal field starts at `field`; place contributors' tails
+    uint64_t pos = field;
+    for (uint32_t j = run_first; j < upto; ++j) {
+      m[j].tail_dst = pos;
+      pos += m[j].trailing;
+    }
+  };
   for (uint32_t k = 0; k < b.segs_per_chunk; ++k) {
     m[k].carry_in = carry;
     m[k].out_off = off;
     if (m[k].nseq) {
-      off += lit_part(m[k].first_lit + carry) + m[k].body;
+      const uint32_t ll = m[k].first_lit + carry;
+      settle(off + 1 + ext_len(ll), k);
+      off += lit_part(ll) + m[k].body;
       carry = m[k].trailing;
+      run_first = k;
     } else {
       carry += m[k].trailing;
     }
   }
-  off += lit_part(carry); // final literal-only sequence
+  // final literal-only sequence carries the pending run
+  settle(off + 1 + ext_len(carry), b.segs_per_chunk);
+  m[b.segs_per_chunk - 1].final_off = off;
+  m[b.segs_per_chunk - 1].final_ll = carry;
+  off += lit_part(carry);
   b.out_sizes[b.id(chunk)] = off;
 }
 
@@ -142,25 +166,24 @@ lz4_emit_k(CodecBatch b, const Seq* seqs, const SegMeta* meta)
   const uint32_t k = uint32_t(seg % b.segs_per_chunk);
   const SegMeta m = meta[seg];
   const bool last = k + 1 == b.segs_per_chunk;
-  if (!m.nseq && !last)
-    return; // its literals travel with the next segment
   const uint8_t* in = b.in + b.id(chunk) * b.in_stride;
   uint8_t* out = b.out + b.id(chunk) * b.out_stride;
   const Seq* s = seqs + seg * kMaxSeqPerSeg;
   const uint32_t s0 = k * kSegBytes;
+  const uint32_t s1 = min(b.chunk_bytes, s0 + kSegBytes);
   uint64_t pos = m.out_off;
-  uint32_t src = s0 - m.carry_in; // first literal of the next sequence
+  uint32_t src = s0; // input position of this segment's next own literal
   for (uint32_t base = 0; base < m.nseq; base += 32) {
     const uint32_t i = base + lane;
     Seq q{ 0, 0, 0 };
-    uint32_t sz = 0;
+    uint32_t sz = 0, carry = 0;
     if (i < m.nseq) {
       q = s[i];
       if (i == 0)
-        q.lit += m.carry_in;
-      sz = lit_part(q.lit) + match_part(q.match);
+        carry = m.carry_in; // written by the segments they came from
+      sz = lit_part(q.lit + carry) + match_part(q.match);
     }
-    // exclusive scans of output size and consumed input
+    // exclusive scans of output size and consumed own input
     uint32_t ex = sz, in_ex = q.lit + q.match;
     for (int o = 1; o < 32; o <<= 1) {
       const uint32_t a = __shfl_up_sync(0xffffffffu, ex, o);
@@ -174,48 +197,45 @@ lz4_emit_k(CodecBatch b, const Seq* seqs, const SegMeta* meta)
     const uint32_t in_tot = __shfl_sync(0xffffffffu, in_ex, 31);
     ex -= sz;
     in_ex -= q.lit + q.match;
+    const uint32_t ll = q.lit + carry;
     uint8_t* o = out + pos + ex;
-    const uint8_t* lits = in + src + in_ex;
+    const uint32_t hdr = 1 + ext_len(ll);
     const bool long_lits = q.lit > 64;
     if (i < m.nseq) {
       const uint32_t ml4 = q.match - 4;
-      *o++ = uint8_t((min(q.lit, 15u) << 4) | min(ml4, 15u));
-      if (q.lit >= 15)
-        o = put_len(o, q.lit - 15);
+      o[0] = uint8_t((min(ll, 15u) << 4) | min(ml4, 15u));
+      if (ll >= 15)
+        put_len(o + 1, ll - 15);
       if (!long_lits)
         for (uint32_t j = 0; j < q.lit; ++j)
-          o[j] = lits[j];
-      o += q.lit;
-      o[0] = uint8_t(q.offset);
-      o[1] = uint8_t(q.offset >> 8);
-      o += 2;
+          o[hdr + carry + j] = in[src + in_ex + j];
+      uint8_t* t = o + hdr + ll;
+      t[0] = uint8_t(q.offset);
+      t[1] = uint8_t(q.offset >> 8);
       if (ml4 >= 15)
-        put_len(o, ml4 - 15);
+        put_len(t + 2, ml4 - 15);
     }
     // long literal runs: copied by the whole warp
     unsigned pending = __ballot_sync(0xffffffffu, i < m.nseq && long_lits);
     while (pending) {
       const int j = __ffs(pending) - 1;
       pending &= pending - 1;
-      const uint32_t ll = __shfl_sync(0xffffffffu, q.lit, j);
+      const uint32_t n = __shfl_sync(0xffffffffu, q.lit, j);
       const uint32_t lo = __shfl_sync(0xffffffffu, ex, j);
       const uint32_t li = __shfl_sync(0xffffffffu, in_ex, j);
-      const uint32_t hdr = 1 + ext_len(ll);
-      warp_bytes(out + pos + lo + hdr, in + src + li, ll);
+      const uint32_t h = __shfl_sync(0xffffffffu, hdr + carry, j);
+      copy_bytes(out + pos + lo + h, in + src + li, n, lane, 32);
     }
     pos += tot;
     src += in_tot;
   }
-  if (last) {
-    // final literal-only sequence: everything from `src` to the chunk end
-    const uint32_t ll = b.chunk_bytes - src;
-    uint8_t* o = out + pos;
-    if (lane == 0) {
-      o[0] = uint8_t(min(ll, 15u) << 4);
-      if (ll >= 15)
-        put_len(o + 1, ll - 15);
-    }
-    warp_bytes(o + 1 + ext_len(ll), in + src, ll);
+  // this segment's trailing literals go into a later literal field
+  copy_bytes(out + m.tail_dst, in + src, s1 - src, lane, 32);
+  if (last && lane == 0) { // header of the final literal-only sequence
+    uint8_t* f = out + m.final_off;
+    f[0] = uint8_t(min(m.final_ll, 15u) << 4);
+    if (m.final_ll >= 15)
+      put_len(f + 1, m.final_ll - 15);
   }
 }
 

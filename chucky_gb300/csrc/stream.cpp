@@ -387,9 +387,11 @@ int Stream::setup_aggregate()
     lut_cap[l] = cap_epochs;
     CK(cudaMalloc(&d_gather[l], lut_n * 4));
     CK(cudaMalloc(&d_perm[l], lut_n * 4));
-    CK(cudaMallocHost(&h_lut_stage[l], 2 * lut_n * 4));
-    CK(cudaMalloc(&d_gather_tmp[l], lut_n * 4));
-    CK(cudaMalloc(&d_perm_tmp[l], lut_n * 4));
+    for (int si = 0; si < 2; ++si) {
+      CK(cudaMallocHost(&h_lut_stage[si][l], 2 * lut_n * 4));
+      CK(cudaMalloc(&d_gather_tmp[si][l], lut_n * 4));
+      CK(cudaMalloc(&d_perm_tmp[si][l], lut_n * 4));
+    }
     planned_count[l] = V.batch_active;
     if (V.batch_active) {
       std::vector<uint32_t> eps(V.batch_active), g(lut_n), pm(lut_n);
@@ -466,9 +468,11 @@ void Stream::release()
     cudaFree(d_chunk_fixed[l]);
     cudaFree(d_gather[l]);
     cudaFree(d_perm[l]);
-    cudaFree(d_gather_tmp[l]);
-    cudaFree(d_perm_tmp[l]);
-    cudaFreeHost(h_lut_stage[l]);
+    for (int si = 0; si < 2; ++si) {
+      cudaFree(d_gather_tmp[si][l]);
+      cudaFree(d_perm_tmp[si][l]);
+      cudaFreeHost(h_lut_stage[si][l]);
+    }
   }
   if (s_copy)
     cudaStreamDestroy(s_copy);
@@ -642,17 +646,17 @@ int Stream::kick_batch(uint32_t n_epochs, const uint32_t* epoch_masks)
     const uint32_t* pm = d_perm[l];
     const uint64_t n = uint64_t(na) * V.layout.chunks_per_epoch;
     if (!planned) {
-      // lut staging is reused: wait for the previous upload from it
-      CK(cudaStreamSynchronize(s_comp));
-      uint32_t* hg = h_lut_stage[l];
-      uint32_t* hp = h_lut_stage[l] + n;
+      // staging of this delivery slot: its previous batch has been
+      // delivered, so its uploads are complete
+      uint32_t* hg = h_lut_stage[si][l];
+      uint32_t* hp = h_lut_stage[si][l] + n;
       build_luts(l, na, eps, hg, hp);
-      CK(cudaMemcpyAsync(d_gather_tmp[l], hg, n * 4, cudaMemcpyHostToDevice,
+      CK(cudaMemcpyAsync(d_gather_tmp[si][l], hg, n * 4, cudaMemcpyHostToDevice,
                          s_comp));
-      CK(cudaMemcpyAsync(d_perm_tmp[l], hp, n * 4, cudaMemcpyHostToDevice,
+      CK(cudaMemcpyAsync(d_perm_tmp[si][l], hp, n * 4, cudaMemcpyHostToDevice,
                          s_comp));
-      g = d_gather_tmp[l];
-      pm = d_perm_tmp[l];
+      g = d_gather_tmp[si][l];
+      pm = d_perm_tmp[si][l];
     }
     AggLevel& A = ab.lv[ab.nlevels++];
     A.gather = g;

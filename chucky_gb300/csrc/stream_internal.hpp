@@ -92,9 +92,9 @@ struct Stream
   // aggregation
   uint32_t* d_gather[LOD_MAX_LEVELS] = {};
   uint32_t* d_perm[LOD_MAX_LEVELS] = {};
-  uint32_t* d_gather_tmp[LOD_MAX_LEVELS] = {};
-  uint32_t* d_perm_tmp[LOD_MAX_LEVELS] = {};
-  uint32_t* h_lut_stage[LOD_MAX_LEVELS] = {};
+  uint32_t* d_gather_tmp[2][LOD_MAX_LEVELS] = {};
+  uint32_t* d_perm_tmp[2][LOD_MAX_LEVELS] = {};
+  uint32_t* h_lut_stage[2][LOD_MAX_LEVELS] = {}; // per delivery slot
   uint32_t lut_cap[LOD_MAX_LEVELS] = {};
   uint32_t planned_count[LOD_MAX_LEVELS] = {};
   uint64_t* d_agg_scratch = nullptr;

@@ -256,28 +256,19 @@ struct Huff
 
 // Code lengths limited to kHufMaxBits, complete prefix code.  Two-queue
 // Huffman on the sorted leaves, then clamp + Kraft repair.
-__device__ bool huff_lengths(const uint32_t* freq, Huff& h)
+__device__ bool huff_lengths(const uint32_t* freq,
+                             const uint16_t* sorted,
+                             int n,
+                             Huff& h)
 {
+  // `sorted`: the n symbols with freq > 0, ascending by (freq, symbol)
   uint16_t sym[256];
   uint32_t f[512];
   int16_t parent[512];
-  int n = 0;
-  for (int s = 0; s < 256; ++s)
-    if (freq[s])
-      sym[n++] = uint16_t(s);
   if (n < 2)
     return false;
-  // insertion sort by (freq, symbol)
-  for (int i = 1; i < n; ++i) {
-    const uint16_t x = sym[i];
-    int j = i;
-    while (j > 0 && (freq[sym[j - 1]] > freq[x] ||
-                     (freq[sym[j - 1]] == freq[x] && sym[j - 1] > x))) {
-      sym[j] = sym[j - 1];
-      --j;
-    }
-    sym[j] = x;
-  }
+  for (int i = 0; i < n; ++i)
+    sym[i] = sorted[i];
   for (int i = 0; i < n; ++i)
     f[i] = freq[sym[i]];
   int leaf = 0, inode = n, next = n;
@@ -543,6 +534,8 @@ struct BlockShared
 {
   uint32_t hist[256];
   uint32_t whist[kSegsPerBlock][256]; // per-warp histograms (merged)
+  uint16_t sorted[256];               // used symbols by (count, symbol)
+  uint32_t nsym;
   Huff huff;
   uint32_t seg_nseq[kSegsPerBlock];
   uint32_t seg_carry[kSegsPerBlock];
@@ -595,7 +588,7 @@ zstd_block_k(CodecBatch b,
       const uint32_t s0 = b0 + k * kSegBytes;
       S.seg_nseq[k] = m.nseq;
       S.seg_carry[k] = carry;
-      S.seg_litout[k] = (s0 - carry - b0) - matched_before;
+      S.seg_litout[k] = (s0 - b0) - matched_before; // literal slot of s0
       matched_before += m.matched;
       nseq += m.nseq;
       carry = m.nseq ? m.trailing : carry + m.trailing;
@@ -624,62 +617,60 @@ zstd_block_k(CodecBatch b,
       S.all_same = 0;
   }
 
-  // gather literals (warp k owns segment k) and histogram them
+  // gather literals: warp k copies the literal bytes that lie inside its
+  // own segment (the bytes before each match and after the last one), so
+  // all warps work even when most segments have no match at all
   if (uint32_t(warp) < nsegs) {
     const uint32_t k = warp;
     const uint32_t s0 = b0 + k * kSegBytes;
+    const uint32_t s1 = min(b1, s0 + kSegBytes);
     const Seq* sq = seqs + (segbase + k) * kMaxSeqPerSeg;
     const uint32_t nq = S.seg_nseq[k];
-    const bool last = k + 1 == nsegs;
-    if (nq || last) {
-      uint32_t src = s0 - S.seg_carry[k]; // input position of next literal
-      uint32_t dst = S.seg_litout[k];
-      for (uint32_t base = 0; base < nq; base += 32) {
-        const uint32_t i = base + lane;
-        uint32_t ll = 0, used = 0;
-        if (i < nq) {
-          const Seq q = sq[i];
-          ll = q.lit + (i == 0 ? S.seg_carry[k] : 0);
-          used = ll + q.match;
-        }
-        uint32_t ex_in = used, ex_out = ll;
-        for (int o = 1; o < 32; o <<= 1) {
-          const uint32_t a = __shfl_up_sync(0xffffffffu, ex_in, o);
-          const uint32_t c = __shfl_up_sync(0xffffffffu, ex_out, o);
-          if (lane >= o) {
-            ex_in += a;
-            ex_out += c;
-          }
-        }
-        const uint32_t tot_in = __shfl_sync(0xffffffffu, ex_in, 31);
-        const uint32_t tot_out = __shfl_sync(0xffffffffu, ex_out, 31);
-        ex_in -= used;
-        ex_out -= ll;
-        // copy every lane's literal run, warp-cooperatively per run
-        unsigned pend = __ballot_sync(0xffffffffu, ll > 0);
-        while (pend) {
-          const int j = __ffs(pend) - 1;
-          pend &= pend - 1;
-          const uint32_t n = __shfl_sync(0xffffffffu, ll, j);
-          const uint32_t si = __shfl_sync(0xffffffffu, ex_in, j);
-          const uint32_t di = __shfl_sync(0xffffffffu, ex_out, j);
-          for (uint32_t t = lane; t < n; t += 32) {
-            const uint8_t c = in[src + si + t];
-            lits[dst + di + t] = c;
-            atomicAdd(&S.whist[warp][c], 1u);
-          }
-        }
-        src += tot_in;
-        dst += tot_out;
+    uint32_t src = s0, dst = S.seg_litout[k];
+    uint32_t* hist = S.whist[warp];
+    for (uint32_t base = 0; base < nq; base += 32) {
+      const uint32_t i = base + lane;
+      uint32_t ll = 0, used = 0;
+      if (i < nq) {
+        const Seq q = sq[i];
+        ll = q.lit; // this segment's own literals (no carry)
+        used = ll + q.match;
       }
-      if (last) {
-        const uint32_t n = b1 - src;
+      uint32_t ex_in = used, ex_out = ll;
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t a = __shfl_up_sync(0xffffffffu, ex_in, o);
+        const uint32_t c = __shfl_up_sync(0xffffffffu, ex_out, o);
+        if (lane >= o) {
+          ex_in += a;
+          ex_out += c;
+        }
+      }
+      const uint32_t tot_in = __shfl_sync(0xffffffffu, ex_in, 31);
+      const uint32_t tot_out = __shfl_sync(0xffffffffu, ex_out, 31);
+      ex_in -= used;
+      ex_out -= ll;
+      unsigned pend = __ballot_sync(0xffffffffu, ll > 0);
+      while (pend) {
+        const int j = __ffs(pend) - 1;
+        pend &= pend - 1;
+        const uint32_t n = __shfl_sync(0xffffffffu, ll, j);
+        const uint32_t si = __shfl_sync(0xffffffffu, ex_in, j);
+        const uint32_t di = __shfl_sync(0xffffffffu, ex_out, j);
         for (uint32_t t = lane; t < n; t += 32) {
-          const uint8_t c = in[src + t];
-          lits[dst + t] = c;
-          atomicAdd(&S.whist[warp][c], 1u);
+          const uint8_t c = in[src + si + t];
+          lits[dst + di + t] = c;
+          atomicAdd(&hist[c], 1u);
         }
       }
+      src += tot_in;
+      dst += tot_out;
+    }
+    // trailing literals of the segment (all of it when nothing matched)
+    const uint32_t n = s1 - src;
+    for (uint32_t t = lane; t < n; t += 32) {
+      const uint8_t c = in[src + t];
+      lits[dst + t] = c;
+      atomicAdd(&hist[c], 1u);
     }
   }
   __syncthreads();
@@ -688,6 +679,26 @@ zstd_block_k(CodecBatch b,
     for (uint32_t w = 0; w < kSegsPerBlock; ++w)
       t += S.whist[w][i];
     S.hist[i] = t;
+  }
+  __syncthreads();
+  // rank the used symbols by (count, symbol) in parallel for the Huffman
+  // build (one comparison pass per symbol instead of a serial sort)
+  for (int i = tid; i < 256; i += blockDim.x) {
+    const uint32_t fi = S.hist[i];
+    if (fi) {
+      int rank = 0;
+      for (int j = 0; j < 256; ++j) {
+        const uint32_t fj = S.hist[j];
+        rank += fj && (fj < fi || (fj == fi && j < i));
+      }
+      S.sorted[rank] = uint16_t(i);
+    }
+  }
+  if (tid == 0) {
+    uint32_t n = 0;
+    for (int i = 0; i < 256; ++i)
+      n += S.hist[i] > 0;
+    S.nsym = n;
   }
   __syncthreads();
 
@@ -700,7 +711,7 @@ zstd_block_k(CodecBatch b,
     S.lit_mode = 0;
     if (nlit > 0 && distinct == 1)
       S.lit_mode = 1;
-    else if (nlit >= 256 && huff_lengths(S.hist, S.huff)) {
+    else if (nlit >= 256 && huff_lengths(S.hist, S.sorted, S.nsym, S.huff)) {
       huff_codes(S.huff);
       uint64_t bits = 0;
       for (int s = 0; s < 256; ++s)
