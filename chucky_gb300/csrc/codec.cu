@@ -33,16 +33,19 @@ int Stream::codec_init()
   return cudaMalloc(&codec_state, bytes) == cudaSuccess ? 0 : 1;
 }
 
-int Stream::codec_compress(uint64_t nchunks, const uint32_t* d_ids)
+int Stream::codec_compress(uint64_t nchunks,
+                           const uint32_t* d_ids,
+                           uint8_t* out,
+                           uint64_t* sizes)
 {
   CodecBatch b{};
   b.in = d_pool;
   b.in_stride = layout.chunk_stride * P.bpe;
   b.chunk_bytes = uint32_t(P.chunk_bytes);
   b.n_chunks = nchunks;
-  b.out = d_comp;
+  b.out = out;
   b.out_stride = comp_stride;
-  b.out_sizes = d_sizes;
+  b.out_sizes = sizes;
   b.level = cfg.codec.level;
   b.chunk_ids = d_ids;
   cudaError_t e = cudaErrorInvalidValue;

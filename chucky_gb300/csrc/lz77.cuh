@@ -63,7 +63,8 @@ __device__ inline SegInfo lz77_parse_segment(const uint8_t* base,
                                              uint32_t start_limit,
                                              uint32_t match_end,
                                              uint16_t* table,
-                                             Seq* out)
+                                             Seq* out,
+                                             uint32_t min_match = 4)
 {
   const int lane = threadIdx.x & 31;
   for (int i = lane; i < (1 << kHashLog); i += 32)
@@ -119,6 +120,10 @@ __device__ inline SegInfo lz77_parse_segment(const uint8_t* base,
       }
       len += __ffs(~eq) - 1;
       break;
+    }
+    if (len < min_match) { // too short to pay for a sequence: literals
+      p = mpos + 1;
+      continue;
     }
     if (lane == 0)
       out[nseq] = Seq{ mpos - lit_start, len, mpos - src };

@@ -125,6 +125,7 @@ int Stream::init(const tile_stream_configuration* c, shard_sink* sk)
   CK(cudaGetDevice(&device));
   CK(cudaStreamCreateWithFlags(&s_copy, cudaStreamNonBlocking));
   CK(cudaStreamCreateWithFlags(&s_comp, cudaStreamNonBlocking));
+  CK(cudaStreamCreateWithFlags(&s_agg, cudaStreamNonBlocking));
   for (auto& t : timers) {
     CK(cudaEventCreate(&t.a));
     CK(cudaEventCreate(&t.b));
@@ -133,6 +134,9 @@ int Stream::init(const tile_stream_configuration* c, shard_sink* sk)
     CK(cudaEventCreateWithFlags(&ev_input_ready[i], cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&ev_input_free[i], cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&ev_batch[i], cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&ev_codec_done[i], cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&ev_agg_done[i], cudaEventDisableTiming));
+    CK(cudaEventRecord(ev_agg_done[i], s_comp));
     CK(cudaMalloc(&d_epoch[i], round_up(P.epoch_bytes, 256) + 256));
     CK(cudaEventRecord(ev_input_free[i], s_comp));
   }
@@ -140,13 +144,17 @@ int Stream::init(const tile_stream_configuration* c, shard_sink* sk)
   CK(cudaMalloc(&d_pool, pool_bytes + 256)); // encoders read 8 B past a chunk
   CK(cudaMemsetAsync(d_pool, 0, pool_bytes, s_comp));
   const uint64_t nchunks = uint64_t(P.K) * P.total_chunks;
-  CK(cudaMalloc(&d_sizes, nchunks * sizeof(uint64_t)));
   if (cfg.codec.id == CODEC_NONE) {
     comp_stride = layout.chunk_stride * P.bpe;
-    CK(launch_fill_u64(d_sizes, P.chunk_bytes, nchunks, s_comp));
+    CK(cudaMalloc(&d_sizes[0], nchunks * sizeof(uint64_t)));
+    d_sizes[1] = d_sizes[0]; // constant: every chunk is chunk_bytes
+    CK(launch_fill_u64(d_sizes[0], P.chunk_bytes, nchunks, s_comp));
   } else {
+    for (int i = 0; i < 2; ++i)
+      CK(cudaMalloc(&d_sizes[i], nchunks * sizeof(uint64_t)));
     comp_stride = round_up(P.max_out, 16);
-    CK(cudaMalloc(&d_comp, nchunks * comp_stride + 64));
+    for (int i = 0; i < 2; ++i)
+      CK(cudaMalloc(&d_comp[i], nchunks * comp_stride + 64));
     if (codec_init())
       return 1;
   }
@@ -421,7 +429,8 @@ int Stream::setup_aggregate()
     for (auto& sh : S.sh)
       sh.index.assign(2 * V.cps_total, ~uint64_t(0));
   }
-  CK(cudaMalloc(&d_agg_scratch, (max_positions + 1) * 8 * size_t(P.nlod)));
+  agg_scratch_slot = (max_positions + 1) * size_t(P.nlod);
+  CK(cudaMalloc(&d_agg_scratch, 2 * agg_scratch_slot * 8));
   return 0;
 }
 
@@ -429,6 +438,8 @@ void Stream::release()
 {
   if (s_comp)
     cudaStreamSynchronize(s_comp);
+  if (s_agg)
+    cudaStreamSynchronize(s_agg);
   if (s_copy)
     cudaStreamSynchronize(s_copy);
   codec_release();
@@ -453,8 +464,18 @@ void Stream::release()
       cudaEventDestroy(t.b);
   }
   cudaFree(d_pool);
-  cudaFree(d_comp);
-  cudaFree(d_sizes);
+  for (int i = 0; i < 2; ++i) {
+    cudaFree(d_comp[i]);
+    if (ev_codec_done[i])
+      cudaEventDestroy(ev_codec_done[i]);
+    if (ev_agg_done[i])
+      cudaEventDestroy(ev_agg_done[i]);
+  }
+  if (s_agg)
+    cudaStreamDestroy(s_agg);
+  if (d_sizes[1] != d_sizes[0])
+    cudaFree(d_sizes[1]);
+  cudaFree(d_sizes[0]);
   cudaFree(d_row_off);
   cudaFree(d_col_off);
   cudaFree(d_values);
@@ -614,18 +635,21 @@ int Stream::kick_batch(uint32_t n_epochs, const uint32_t* epoch_masks)
                          s_comp));
       d_ids = d_chunk_ids[si];
     }
+    // the aggregation that read this compressed slot two batches ago must
+    // be done before the encoders overwrite it
+    CK(cudaStreamWaitEvent(s_comp, ev_agg_done[si], 0));
     if (timed_begin(s_comp, &metrics.compress, double(n * P.chunk_bytes), 0))
       return 1;
-    if (codec_compress(n, d_ids))
+    if (codec_compress(n, d_ids, d_comp[si], d_sizes[si]))
       return 1;
     if (timed_end(s_comp))
       return 1;
-    comp = d_comp;
+    comp = d_comp[si];
   }
   AggBatch ab{};
   ab.comp = comp;
   ab.comp_stride = comp_stride;
-  ab.sizes = d_sizes;
+  ab.sizes = d_sizes[si];
   ab.alignment = cfg.shard_alignment;
   S.n_levels = 0;
   for (int l = 0; l < P.nlod; ++l) {
@@ -675,12 +699,23 @@ int Stream::kick_batch(uint32_t n_epochs, const uint32_t* epoch_masks)
   if (sink->wait_fence)
     for (int k = 0; k < S.n_levels; ++k)
       sink->wait_fence(sink, uint8_t(S.level_of[k]), S.fence[S.level_of[k]]);
-  if (timed_begin(s_comp, &metrics.aggregate, 0, 0))
+  // Compressed input: aggregate on its own stream (bound by the host link)
+  // so the next batch's LOD and encoders overlap with it.  Uncompressed
+  // input reads the chunk pool itself and stays in order on the compute
+  // stream.
+  cudaStream_t sa = s_comp;
+  if (cfg.codec.id != CODEC_NONE) {
+    CK(cudaEventRecord(ev_codec_done[si], s_comp));
+    CK(cudaStreamWaitEvent(s_agg, ev_codec_done[si], 0));
+    sa = s_agg;
+  }
+  if (timed_begin(sa, &metrics.aggregate, 0, 0))
     return 1;
-  CK(launch_aggregate(ab, d_agg_scratch, s_comp));
-  if (timed_end(s_comp))
+  CK(launch_aggregate(ab, d_agg_scratch + si * agg_scratch_slot, sa));
+  if (timed_end(sa))
     return 1;
-  CK(cudaEventRecord(ev_batch[si], s_comp));
+  CK(cudaEventRecord(ev_agg_done[si], sa));
+  CK(cudaEventRecord(ev_batch[si], sa));
   S.busy = 1;
   S.seq = ++batch_seq;
   next_slot ^= 1;
@@ -1039,6 +1074,7 @@ tile_stream_gpu_restart(tile_stream_gpu* s, shard_sink* sink)
   if (I.cursor != 0 && !I.flushed)
     return 1;
   if (cudaStreamSynchronize(I.s_comp) != cudaSuccess ||
+      cudaStreamSynchronize(I.s_agg) != cudaSuccess ||
       cudaStreamSynchronize(I.s_copy) != cudaSuccess)
     return 1;
   if (sink)

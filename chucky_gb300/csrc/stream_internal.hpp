@@ -60,8 +60,10 @@ struct Stream
 
   // chunk pool / compression
   uint8_t* d_pool = nullptr;
-  uint8_t* d_comp = nullptr;
-  uint64_t* d_sizes = nullptr;
+  uint8_t* d_comp[2] = {}; // compressed slots, one per delivery slot
+  cudaStream_t s_agg = nullptr; // aggregation (host-link bound) stream
+  cudaEvent_t ev_codec_done[2] = {}, ev_agg_done[2] = {};
+  uint64_t* d_sizes[2] = {}; // compressed sizes, one per delivery slot
   uint64_t comp_stride = 0;
   void* codec_state = nullptr;
   uint32_t* h_chunk_ids[2] = {};   // pinned staging of the encode list
@@ -98,6 +100,7 @@ struct Stream
   uint32_t lut_cap[LOD_MAX_LEVELS] = {};
   uint32_t planned_count[LOD_MAX_LEVELS] = {};
   uint64_t* d_agg_scratch = nullptr;
+  uint64_t agg_scratch_slot = 0; // entries per delivery slot
   DeliverySlot slot[2];
   cudaEvent_t ev_batch[2] = {};
   int next_slot = 0;
@@ -147,7 +150,10 @@ struct Stream
   writer_result flush();
 
   int codec_init();
-  int codec_compress(uint64_t nchunks, const uint32_t* d_ids);
+  int codec_compress(uint64_t nchunks,
+                     const uint32_t* d_ids,
+                     uint8_t* out,
+                     uint64_t* sizes);
   void codec_release();
 
   int timed_begin(cudaStream_t st, stream_metric* m, double in, double out);

@@ -27,13 +27,22 @@ namespace chucky {
 
 namespace {
 
-constexpr uint32_t kBlockLog = 17;
-constexpr uint32_t kBlockBytes = 1u << kBlockLog; // 128 KiB
+// 32 KiB blocks: every block builds its own Huffman table serially, so
+// smaller blocks put more of them in flight (the table costs ~0.3% ratio)
+constexpr uint32_t kBlockLog = 15;
+constexpr uint32_t kBlockBytes = 1u << kBlockLog; // 32 KiB
 constexpr uint32_t kSegsPerBlock = kBlockBytes / kSegBytes;
 constexpr uint32_t kStageBytes = kBlockBytes + 1024;
-constexpr int kBlockThreads = 32 * kSegsPerBlock; // a warp per segment
+constexpr int kStreamThreads = 32;                // a warp per Huffman stream
+constexpr int kBlockThreads = 4 * kStreamThreads; // >= a warp per segment
+static_assert(kBlockThreads >= 32 * int(kSegsPerBlock), "warp per segment");
 constexpr int kFindWarps = 4;
 constexpr uint32_t kHufMaxBits = 11;
+#ifndef CHUCKY_ZSTD_MIN_MATCH
+#define CHUCKY_ZSTD_MIN_MATCH 6
+#endif
+// matches shorter than this cost more as a sequence than as literals
+constexpr uint32_t kMinMatch = CHUCKY_ZSTD_MIN_MATCH;
 
 struct ZSeg
 {
@@ -228,7 +237,8 @@ zstd_find_k(CodecBatch b, Seq* seqs, ZSeg* meta)
   const uint32_t s0 = k * kSegBytes;
   const uint32_t s1 = min(b.chunk_bytes, s0 + kSegBytes);
   Seq* out = seqs + seg * kMaxSeqPerSeg;
-  const SegInfo info = lz77_parse_segment(base, s0, s1, s1, s1, tables[w], out);
+  const SegInfo info =
+    lz77_parse_segment(base, s0, s1, s1, s1, tables[w], out, kMinMatch);
   __syncwarp();
   uint32_t matched = 0;
   for (uint32_t i = lane; i < info.nseq; i += 32)
@@ -242,6 +252,18 @@ zstd_find_k(CodecBatch b, Seq* seqs, ZSeg* meta)
 // ---------------------------------------------------------------------------
 // Huffman (thread 0 of the block CTA)
 // ---------------------------------------------------------------------------
+
+// Working arrays of the serial Huffman build, kept in shared memory (local
+// memory of one thread is interleaved with every other thread's frame and
+// would miss L1 on every access).
+struct HuffScratch
+{
+  uint16_t sym[256];
+  uint32_t f[512];
+  int16_t parent[512];
+  uint8_t depth[512];
+  uint8_t w[256];
+};
 
 struct Huff
 {
@@ -259,12 +281,13 @@ struct Huff
 __device__ bool huff_lengths(const uint32_t* freq,
                              const uint16_t* sorted,
                              int n,
-                             Huff& h)
+                             Huff& h,
+                             HuffScratch& x)
 {
   // `sorted`: the n symbols with freq > 0, ascending by (freq, symbol)
-  uint16_t sym[256];
-  uint32_t f[512];
-  int16_t parent[512];
+  uint16_t* sym = x.sym;
+  uint32_t* f = x.f;
+  int16_t* parent = x.parent;
   if (n < 2)
     return false;
   for (int i = 0; i < n; ++i)
@@ -284,7 +307,7 @@ __device__ bool huff_lengths(const uint32_t* freq,
     parent[pick[0]] = parent[pick[1]] = int16_t(next);
     ++next;
   }
-  uint8_t depth[512];
+  uint8_t* depth = x.depth;
   depth[next - 1] = 0;
   for (int i = next - 2; i >= 0; --i)
     depth[i] = uint8_t(depth[parent[i]] + 1);
@@ -394,15 +417,11 @@ __device__ void norm_weights(const uint32_t* hist, int nsym, int al, int16_t* no
   }
   while (sum < size) { // give to the most under-represented that has room
     int best = -1;
-    double bestr = -1;
     for (int s = 0; s < nsym; ++s)
-      if (hist[s] && norm[s] < half) {
-        const double r = double(hist[s]) / norm[s];
-        if (r > bestr) {
-          bestr = r;
-          best = s;
-        }
-      }
+      if (hist[s] && norm[s] < half &&
+          (best < 0 || uint64_t(hist[s]) * uint64_t(norm[best]) >
+                         uint64_t(hist[best]) * uint64_t(norm[s])))
+        best = s;
     if (best < 0) // everything capped: an absent symbol takes the rest
       for (int s = 0; s < nsym && best < 0; ++s)
         if (!hist[s] && norm[s] < half)
@@ -469,10 +488,10 @@ __device__ int write_ncount(uint8_t* out, const int16_t* norm, int nsym, int al)
 }
 
 // Tree description: direct 4-bit weights when <= 128 weights, else FSE.
-__device__ bool huff_describe(Huff& h)
+__device__ bool huff_describe(Huff& h, HuffScratch& x, FseEnc& t)
 {
   const int mb = h.max_bits, nw = h.last; // explicit weights: symbols < last
-  uint8_t w[256];
+  uint8_t* w = x.w;
   for (int s = 0; s < nw; ++s)
     w[s] = h.len[s] ? uint8_t(mb + 1 - h.len[s]) : 0;
   if (nw <= 128) {
@@ -495,7 +514,6 @@ __device__ bool huff_describe(Huff& h)
   int16_t norm[16];
   const int al = 6;
   norm_weights(hist, nsym, al, norm);
-  FseEnc t;
   fse_build(t, norm, nsym, al);
   uint8_t* out = h.desc + 1;
   int len = write_ncount(out, norm, nsym, al);
@@ -536,6 +554,9 @@ struct BlockShared
   uint32_t whist[kSegsPerBlock][256]; // per-warp histograms (merged)
   uint16_t sorted[256];               // used symbols by (count, symbol)
   uint32_t nsym;
+  FseEnc tll, tml, tof;               // predefined sequence tables
+  FseEnc tw;                          // Huffman weights table
+  HuffScratch hx;
   Huff huff;
   uint32_t seg_nseq[kSegsPerBlock];
   uint32_t seg_carry[kSegsPerBlock];
@@ -555,11 +576,45 @@ __device__ __forceinline__ void put_le(uint8_t* p, uint64_t v, int n)
     p[i] = uint8_t(v >> (8 * i));
 }
 
+// Copy n literal bytes in[src..) -> lits[dst..) with one warp and count them
+// in `hist`; the body moves whole aligned 32-bit words of the input.
+__device__ __forceinline__ void gather_run(const uint8_t* in,
+                                           uint32_t src,
+                                           uint32_t n,
+                                           uint8_t* lits,
+                                           uint32_t dst,
+                                           uint32_t* hist,
+                                           unsigned lane)
+{
+  const uint32_t lead = (4 - (src & 3)) & 3;
+  const uint32_t h = n < lead ? n : lead;
+  if (lane < h) {
+    const uint8_t c = in[src + lane];
+    lits[dst + lane] = c;
+    atomicAdd(&hist[c], 1u);
+  }
+  const uint32_t nw = (n - h) >> 2;
+  const uint32_t* w = reinterpret_cast<const uint32_t*>(in + src + h);
+  for (uint32_t i = lane; i < nw; i += 32) {
+    const uint32_t v = w[i];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const uint8_t c = uint8_t(v >> (8 * k));
+      lits[dst + h + 4 * i + k] = c;
+      atomicAdd(&hist[c], 1u);
+    }
+  }
+  for (uint32_t t = h + 4 * nw + lane; t < n; t += 32) {
+    const uint8_t c = in[src + t];
+    lits[dst + t] = c;
+    atomicAdd(&hist[c], 1u);
+  }
+}
+
 __global__ void __launch_bounds__(kBlockThreads)
 zstd_block_k(CodecBatch b,
              const Seq* seqs,
              const ZSeg* meta,
-             uint8_t* lits_all,
              uint8_t* stage_all,
              uint32_t* block_sizes,
              uint32_t blocks_per_chunk)
@@ -576,11 +631,18 @@ zstd_block_k(CodecBatch b,
   const uint32_t seg0 = b0 / kSegBytes;
   const uint32_t nsegs = (bsize + kSegBytes - 1) / kSegBytes;
   const uint64_t segbase = chunk * b.segs_per_chunk + seg0;
-  uint8_t* lits = lits_all + blk * kBlockBytes;
+  CHUCKY_DYN_SHARED(uint8_t, lits); // this block's literals
   uint8_t* stage = stage_all + blk * kStageBytes;
 
   for (int i = tid; i < 256 * int(kSegsPerBlock); i += blockDim.x)
     (&S.whist[0][0])[i] = 0;
+  // the three predefined sequence tables, one thread each
+  if (tid == 32)
+    fse_build(S.tll, kLLNorm, 36, 6);
+  else if (tid == 64)
+    fse_build(S.tml, kMLNorm, 53, 6);
+  else if (tid == 96)
+    fse_build(S.tof, kOFNorm, 29, 5);
   if (tid == 0) {
     uint32_t carry = 0, matched_before = 0, nseq = 0;
     for (uint32_t k = 0; k < nsegs; ++k) {
@@ -656,22 +718,13 @@ zstd_block_k(CodecBatch b,
         const uint32_t n = __shfl_sync(0xffffffffu, ll, j);
         const uint32_t si = __shfl_sync(0xffffffffu, ex_in, j);
         const uint32_t di = __shfl_sync(0xffffffffu, ex_out, j);
-        for (uint32_t t = lane; t < n; t += 32) {
-          const uint8_t c = in[src + si + t];
-          lits[dst + di + t] = c;
-          atomicAdd(&hist[c], 1u);
-        }
+        gather_run(in, src + si, n, lits, dst + di, hist, lane);
       }
       src += tot_in;
       dst += tot_out;
     }
     // trailing literals of the segment (all of it when nothing matched)
-    const uint32_t n = s1 - src;
-    for (uint32_t t = lane; t < n; t += 32) {
-      const uint8_t c = in[src + t];
-      lits[dst + t] = c;
-      atomicAdd(&hist[c], 1u);
-    }
+    gather_run(in, src, s1 - src, lits, dst, hist, lane);
   }
   __syncthreads();
   for (int i = tid; i < 256; i += blockDim.x) {
@@ -711,14 +764,14 @@ zstd_block_k(CodecBatch b,
     S.lit_mode = 0;
     if (nlit > 0 && distinct == 1)
       S.lit_mode = 1;
-    else if (nlit >= 256 && huff_lengths(S.hist, S.sorted, S.nsym, S.huff)) {
+    else if (nlit >= 256 && huff_lengths(S.hist, S.sorted, S.nsym, S.huff, S.hx)) {
       huff_codes(S.huff);
       uint64_t bits = 0;
       for (int s = 0; s < 256; ++s)
         bits += uint64_t(S.hist[s]) * S.huff.len[s];
       S.huff.bits = bits;
       // rough size: description + jump table + header + streams
-      if (bits / 8 + 160 < nlit && huff_describe(S.huff))
+      if (bits / 8 + 160 < nlit && huff_describe(S.huff, S.hx, S.tw))
         S.lit_mode = 2;
     }
   }
@@ -727,25 +780,26 @@ zstd_block_k(CodecBatch b,
   // ---- Huffman streams: bit lengths per stream (64 threads per stream)
   const uint32_t per = (nlit + 3) / 4;
   if (S.lit_mode == 2) {
-    const int st = tid >> 6, t = tid & 63; // stream, thread within stream
+    const int st = tid / kStreamThreads, t = tid % kStreamThreads;
     const uint32_t a0 = st * per;
     const uint32_t a1 = st == 3 ? nlit : min(nlit, a0 + per);
     const uint32_t m = a1 - a0;
     // this thread's share of the stream in writing order (reversed)
-    const uint32_t q0 = uint32_t(uint64_t(m) * t / 64);
-    const uint32_t q1 = uint32_t(uint64_t(m) * (t + 1) / 64);
+    const uint32_t q0 = uint32_t(uint64_t(m) * t / kStreamThreads);
+    const uint32_t q1 = uint32_t(uint64_t(m) * (t + 1) / kStreamThreads);
     uint32_t bits = 0;
     for (uint32_t r = q0; r < q1; ++r)
       bits += S.huff.len[lits[a1 - 1 - r]];
-    // exclusive scan over the stream's 64 threads (2 warps)
-    __shared__ uint32_t part[kBlockThreads];
-    part[tid] = bits;
-    __syncthreads();
-    uint32_t before = 0;
-    for (int u = 0; u < t; ++u)
-      before += part[(st << 6) + u];
-    if (t == 63)
-      S.stream_bits[st] = before + bits;
+    // exclusive scan over the stream's warp
+    uint32_t before = bits;
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, before, o);
+      if (t >= o)
+        before += y;
+    }
+    if (t == kStreamThreads - 1)
+      S.stream_bits[st] = before;
+    before -= bits;
     __syncthreads();
     if (tid == 0) {
       // literals section layout
@@ -820,7 +874,7 @@ zstd_block_k(CodecBatch b,
           ++word;
         }
       }
-      if (t == 63) { // end mark after the stream's last bit
+      if (t == kStreamThreads - 1) { // end mark after the stream's last bit
         acc |= uint64_t(1) << fill;
         fill += 1;
         if (fill >= 32) {
@@ -888,10 +942,9 @@ zstd_block_k(CodecBatch b,
     }
     if (nseq && fits) {
       *o++ = 0; // predefined LL, OF and ML tables
-      FseEnc tll, tml, tof;
-      fse_build(tll, kLLNorm, 36, 6);
-      fse_build(tml, kMLNorm, 53, 6);
-      fse_build(tof, kOFNorm, 29, 5);
+      const FseEnc& tll = S.tll;
+      const FseEnc& tml = S.tml;
+      const FseEnc& tof = S.tof;
       BitOut bo;
       bo.init(o);
       // walk the sequences backwards across segments
@@ -1006,7 +1059,7 @@ size_t zstd_scratch_bytes(uint64_t n_chunks, uint32_t chunk_bytes)
   const uint64_t blocks =
     n_chunks * ((chunk_bytes + kBlockBytes - 1) / kBlockBytes);
   return segs * (kMaxSeqPerSeg * sizeof(Seq) + sizeof(ZSeg)) +
-         blocks * (kBlockBytes + kStageBytes + sizeof(uint32_t)) + 1024;
+         blocks * (kStageBytes + sizeof(uint32_t)) + 1024;
 }
 
 cudaError_t launch_zstd(CodecBatch b, void* scratch, cudaStream_t st)
@@ -1025,8 +1078,6 @@ cudaError_t launch_zstd(CodecBatch b, void* scratch, cudaStream_t st)
   ZSeg* meta = reinterpret_cast<ZSeg*>(p);
   p += segs * sizeof(ZSeg);
   p = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(p) + 255) & ~uintptr_t(255));
-  uint8_t* lits = p;
-  p += blocks * kBlockBytes;
   uint8_t* stage = p;
   p += blocks * kStageBytes;
   uint32_t* bsizes = reinterpret_cast<uint32_t*>(p);
@@ -1035,7 +1086,7 @@ cudaError_t launch_zstd(CodecBatch b, void* scratch, cudaStream_t st)
   CHUCKY_LAUNCH(zstd_find_k, unsigned((segs + kFindWarps - 1) / kFindWarps), 32 * kFindWarps, 0, st, b, seqs, meta);
   if ((e = cudaGetLastError()) != cudaSuccess)
     return e;
-  CHUCKY_LAUNCH(zstd_block_k, unsigned(blocks), kBlockThreads, 0, st, b, seqs, meta, lits,
+  CHUCKY_LAUNCH(zstd_block_k, unsigned(blocks), kBlockThreads, kBlockBytes + 16, st, b, seqs, meta,
                                                            stage, bsizes, bpc);
   if ((e = cudaGetLastError()) != cudaSuccess)
     return e;

@@ -191,6 +191,7 @@ void launch(unsigned grid, unsigned block, const std::function<void()>& body);
 
 } // namespace simt
 
+#define CHUCKY_DYN_SHARED(T, name) static T name[1 << 20]
 #define CHUCKY_LAUNCH(kernel, grid, block, smem, stream, ...)                  \
   simt::launch(unsigned(grid), unsigned(block), [&] { kernel(__VA_ARGS__); })
 
