@@ -70,14 +70,40 @@ __device__ inline SegInfo lz77_parse_segment(const uint8_t* base,
   for (int i = lane; i < (1 << kHashLog); i += 32)
     table[i] = 0xFFFF;
   __syncwarp();
+  // The bytes under the 32 probed positions come from a 256-byte window
+  // held in registers (lane i: words i and 32+i), refilled with coalesced
+  // 128-byte warp loads, so probing costs no memory latency.
+  const uint32_t* wbase = reinterpret_cast<const uint32_t*>(base);
+  uint32_t win = s0 & ~3u; // byte position of the window start
+  uint32_t cur = __ldg(wbase + (win >> 2) + lane);
+  uint32_t nxt = __ldg(wbase + (win >> 2) + 32 + lane);
   uint32_t p = s0, lit_start = s0, nseq = 0;
   while (p < start_limit) {
+    if (p >= win + 128) { // slide (or jump) the window
+      if (p < win + 256) {
+        cur = nxt;
+        win += 128;
+        nxt = __ldg(wbase + (win >> 2) + 32 + lane);
+      } else {
+        win = p & ~3u;
+        cur = __ldg(wbase + (win >> 2) + lane);
+        nxt = __ldg(wbase + (win >> 2) + 32 + lane);
+      }
+    }
     const uint32_t q = p + lane;
     const bool valid = q < start_limit && q + 4 <= match_end;
+    // words j and j+1 of the window hold bytes [q, q+4)
+    const uint32_t j = (q - win) >> 2; // <= 63 - 1 since p < win + 128
+    const uint32_t a0 = __shfl_sync(0xffffffffu, cur, j & 31);
+    const uint32_t b0 = __shfl_sync(0xffffffffu, nxt, j & 31);
+    const uint32_t a1 = __shfl_sync(0xffffffffu, cur, (j + 1) & 31);
+    const uint32_t b1 = __shfl_sync(0xffffffffu, nxt, (j + 1) & 31);
+    const uint32_t lo = j < 32 ? a0 : b0;
+    const uint32_t hi = (j + 1) < 32 ? a1 : b1;
     uint32_t v = 0, h = 0, cand = 0xFFFFFFFFu;
     bool ok = false;
     if (valid) {
-      v = load_u32(base, q);
+      v = __funnelshift_r(lo, hi, (q & 3) * 8);
       h = hash4(v);
       const uint16_t t = table[h];
       // entries can be ahead of q: positions probed in an earlier step

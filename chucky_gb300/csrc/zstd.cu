@@ -111,10 +111,16 @@ struct FseEnc
 };
 
 // Build encoder tables from normalized counts (-1 = "less than 1").
-__device__ void fse_build(FseEnc& t, const int16_t* norm, int nsym, int al)
+// `spread` and `fill` are 64-entry scratch arrays (shared memory on the
+// device: local arrays of one thread would miss L1).
+__host__ __device__ inline void fse_build(FseEnc& t,
+                                          const int16_t* norm,
+                                          int nsym,
+                                          int al,
+                                          uint8_t* spread,
+                                          uint8_t* fill)
 {
   const int size = 1 << al;
-  uint8_t spread[64];
   int high = size - 1;
   for (int s = 0; s < nsym; ++s)
     if (norm[s] == -1)
@@ -134,13 +140,18 @@ __device__ void fse_build(FseEnc& t, const int16_t* norm, int nsym, int al)
     t.first[s] = uint8_t(acc);
     acc += t.count[s];
   }
-  uint8_t fill[64];
   for (int s = 0; s < nsym; ++s)
     fill[s] = t.first[s];
   for (int u = 0; u < size; ++u)
     t.states[fill[spread[u]]++] = uint8_t(u);
   t.al = al;
 }
+
+// The three predefined sequence tables, built once on the host.
+struct PredefTables
+{
+  FseEnc ll, ml, of;
+};
 
 // v in [size, 2 size): emit bits, move to a state of symbol s.
 __device__ __forceinline__ void fse_encode(const FseEnc& t,
@@ -163,14 +174,14 @@ __device__ __forceinline__ uint32_t fse_init(const FseEnc& t, int s)
 }
 
 // Predefined distributions (RFC 8878 3.1.1.3.2.2).
-__constant__ int16_t kLLNorm[36] = { 4, 3, 2, 2, 2, 2, 2, 2, 2, 2, 2, 2,
+static const int16_t kLLNormH[36] = { 4, 3, 2, 2, 2, 2, 2, 2, 2, 2, 2, 2,
                                      2, 1, 1, 1, 2, 2, 2, 2, 2, 2, 2, 2,
                                      2, 3, 2, 1, 1, 1, 1, 1, -1, -1, -1, -1 };
-__constant__ int16_t kMLNorm[53] = { 1, 4, 3, 2, 2, 2, 2, 2, 2, 1, 1, 1, 1, 1,
+static const int16_t kMLNormH[53] = { 1, 4, 3, 2, 2, 2, 2, 2, 2, 1, 1, 1, 1, 1,
                                      1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1,
                                      1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1,
                                      1, 1, 1, 1, -1, -1, -1, -1, -1, -1, -1 };
-__constant__ int16_t kOFNorm[29] = { 1, 1, 1, 1, 1, 1, 2, 2, 2, 1,
+static const int16_t kOFNormH[29] = { 1, 1, 1, 1, 1, 1, 2, 2, 2, 1,
                                      1, 1, 1, 1, 1, 1, 1, 1, 1, 1,
                                      1, 1, 1, 1, -1, -1, -1, -1, -1 };
 
@@ -258,6 +269,9 @@ zstd_find_k(CodecBatch b, Seq* seqs, ZSeg* meta)
 // would miss L1 on every access).
 struct HuffScratch
 {
+  uint32_t rank_start[16], count_w[16], whist[16];
+  int16_t norm[16];
+  uint8_t spread[64], fill[64];
   uint16_t sym[256];
   uint32_t f[512];
   int16_t parent[512];
@@ -267,6 +281,7 @@ struct HuffScratch
 
 struct Huff
 {
+  uint32_t cl[256];    // code | length << 16 (one load per symbol)
   uint16_t code[256];
   uint8_t len[256];
   int max_bits;
@@ -354,11 +369,11 @@ __device__ bool huff_lengths(const uint32_t* freq,
 
 // Canonical codes in zstd's order: by weight ascending (longest code
 // first), then by symbol (RFC 8878 4.2.1.3).
-__device__ void huff_codes(Huff& h)
+__device__ void huff_codes(Huff& h, uint32_t* rank_start, uint32_t* count_w)
 {
   const int mb = h.max_bits;
-  uint32_t rank_start[16] = { 0 };
-  uint32_t count_w[16] = { 0 };
+  for (int i = 0; i < 16; ++i)
+    rank_start[i] = count_w[i] = 0;
   for (int s = 0; s < 256; ++s)
     if (h.len[s])
       count_w[mb + 1 - h.len[s]]++;
@@ -504,17 +519,19 @@ __device__ bool huff_describe(Huff& h, HuffScratch& x, FseEnc& t)
     return true;
   }
   // FSE-compressed weights, accuracy log 6, two interleaved states
-  uint32_t hist[16] = { 0 };
+  uint32_t* hist = x.whist;
+  for (int i = 0; i < 16; ++i)
+    hist[i] = 0;
   int maxw = 0;
   for (int s = 0; s < nw; ++s) {
     hist[w[s]]++;
     maxw = w[s] > maxw ? w[s] : maxw;
   }
   const int nsym = maxw + 2 <= 13 ? maxw + 2 : 13; // room for a spare symbol
-  int16_t norm[16];
+  int16_t* norm = x.norm;
   const int al = 6;
   norm_weights(hist, nsym, al, norm);
-  fse_build(t, norm, nsym, al);
+  fse_build(t, norm, nsym, al, x.spread, x.fill);
   uint8_t* out = h.desc + 1;
   int len = write_ncount(out, norm, nsym, al);
   BitOut bo;
@@ -554,7 +571,7 @@ struct BlockShared
   uint32_t whist[kSegsPerBlock][256]; // per-warp histograms (merged)
   uint16_t sorted[256];               // used symbols by (count, symbol)
   uint32_t nsym;
-  FseEnc tll, tml, tof;               // predefined sequence tables
+  PredefTables pre;                   // predefined sequence tables
   FseEnc tw;                          // Huffman weights table
   HuffScratch hx;
   Huff huff;
@@ -574,6 +591,28 @@ __device__ __forceinline__ void put_le(uint8_t* p, uint64_t v, int n)
 {
   for (int i = 0; i < n; ++i)
     p[i] = uint8_t(v >> (8 * i));
+}
+
+// Visit lits[hi-1], lits[hi-2], ..., lits[lo] (descending), reading the
+// shared-memory literal buffer 16 bytes at a time.
+template<typename F>
+__device__ __forceinline__ void for_each_desc(const uint8_t* lits,
+                                              uint32_t lo,
+                                              uint32_t hi,
+                                              F&& f)
+{
+  uint32_t a = hi;
+  while (a > lo) {
+    const uint32_t wi = (a - 1) >> 4;
+    const uint4 w = reinterpret_cast<const uint4*>(lits)[wi];
+    const uint32_t wlo = max(lo, wi << 4);
+    for (uint32_t x = a; x > wlo; --x) {
+      const uint32_t o = (x - 1) & 15;
+      const uint32_t word = o < 4 ? w.x : (o < 8 ? w.y : (o < 12 ? w.z : w.w));
+      f(uint8_t(word >> ((o & 3) * 8)));
+    }
+    a = wlo;
+  }
 }
 
 // Copy n literal bytes in[src..) -> lits[dst..) with one warp and count them
@@ -613,6 +652,7 @@ __device__ __forceinline__ void gather_run(const uint8_t* in,
 
 __global__ void __launch_bounds__(kBlockThreads)
 zstd_block_k(CodecBatch b,
+             const __grid_constant__ PredefTables pre,
              const Seq* seqs,
              const ZSeg* meta,
              uint8_t* stage_all,
@@ -636,13 +676,13 @@ zstd_block_k(CodecBatch b,
 
   for (int i = tid; i < 256 * int(kSegsPerBlock); i += blockDim.x)
     (&S.whist[0][0])[i] = 0;
-  // the three predefined sequence tables, one thread each
-  if (tid == 32)
-    fse_build(S.tll, kLLNorm, 36, 6);
-  else if (tid == 64)
-    fse_build(S.tml, kMLNorm, 53, 6);
-  else if (tid == 96)
-    fse_build(S.tof, kOFNorm, 29, 5);
+  // the three predefined sequence tables (built once on the host)
+  {
+    const uint32_t* src = reinterpret_cast<const uint32_t*>(&pre);
+    uint32_t* dst = reinterpret_cast<uint32_t*>(&S.pre);
+    for (int i = tid; i < int(sizeof(PredefTables) / 4); i += blockDim.x)
+      dst[i] = src[i];
+  }
   if (tid == 0) {
     uint32_t carry = 0, matched_before = 0, nseq = 0;
     for (uint32_t k = 0; k < nsegs; ++k) {
@@ -757,24 +797,20 @@ zstd_block_k(CodecBatch b,
 
   const uint32_t nlit = S.nlit, nseq = S.nseq;
   if (tid == 0) {
-    // literals section mode
-    int distinct = 0;
-    for (int s = 0; s < 256; ++s)
-      distinct += S.hist[s] > 0;
+    // literals section mode (the exact Huffman size decides below)
     S.lit_mode = 0;
-    if (nlit > 0 && distinct == 1)
+    if (nlit > 0 && S.nsym == 1)
       S.lit_mode = 1;
-    else if (nlit >= 256 && huff_lengths(S.hist, S.sorted, S.nsym, S.huff, S.hx)) {
-      huff_codes(S.huff);
-      uint64_t bits = 0;
-      for (int s = 0; s < 256; ++s)
-        bits += uint64_t(S.hist[s]) * S.huff.len[s];
-      S.huff.bits = bits;
-      // rough size: description + jump table + header + streams
-      if (bits / 8 + 160 < nlit && huff_describe(S.huff, S.hx, S.tw))
+    else if (nlit >= 256 &&
+             huff_lengths(S.hist, S.sorted, S.nsym, S.huff, S.hx)) {
+      huff_codes(S.huff, S.hx.rank_start, S.hx.count_w);
+      if (huff_describe(S.huff, S.hx, S.tw))
         S.lit_mode = 2;
     }
   }
+  __syncthreads();
+  for (int c = tid; c < 256; c += blockDim.x)
+    S.huff.cl[c] = uint32_t(S.huff.code[c]) | (uint32_t(S.huff.len[c]) << 16);
   __syncthreads();
 
   // ---- Huffman streams: bit lengths per stream (64 threads per stream)
@@ -788,8 +824,9 @@ zstd_block_k(CodecBatch b,
     const uint32_t q0 = uint32_t(uint64_t(m) * t / kStreamThreads);
     const uint32_t q1 = uint32_t(uint64_t(m) * (t + 1) / kStreamThreads);
     uint32_t bits = 0;
-    for (uint32_t r = q0; r < q1; ++r)
-      bits += S.huff.len[lits[a1 - 1 - r]];
+    const uint32_t* cl = S.huff.cl;
+    for_each_desc(lits, a1 - q1, a1 - q0,
+                  [&](uint8_t c) { bits += cl[c] >> 16; });
     // exclusive scan over the stream's warp
     uint32_t before = bits;
     for (int o = 1; o < 32; o <<= 1) {
@@ -859,10 +896,11 @@ zstd_block_k(CodecBatch b,
       const bool first_shared = fill != 0;
       bool first = true;
       uint64_t acc = 0;
-      for (uint32_t r = q0; r < q1; ++r) {
-        const uint8_t c = lits[a1 - 1 - r];
-        acc |= uint64_t(S.huff.code[c]) << fill;
-        fill += S.huff.len[c];
+      const uint32_t* cl = S.huff.cl;
+      for_each_desc(lits, a1 - q1, a1 - q0, [&](uint8_t c) {
+        const uint32_t e = cl[c];
+        acc |= uint64_t(e & 0xFFFF) << fill;
+        fill += int(e >> 16);
         if (fill >= 32) {
           if (first && first_shared)
             atomicOr(wbase + word, uint32_t(acc));
@@ -873,7 +911,7 @@ zstd_block_k(CodecBatch b,
           fill -= 32;
           ++word;
         }
-      }
+      });
       if (t == kStreamThreads - 1) { // end mark after the stream's last bit
         acc |= uint64_t(1) << fill;
         fill += 1;
@@ -942,9 +980,9 @@ zstd_block_k(CodecBatch b,
     }
     if (nseq && fits) {
       *o++ = 0; // predefined LL, OF and ML tables
-      const FseEnc& tll = S.tll;
-      const FseEnc& tml = S.tml;
-      const FseEnc& tof = S.tof;
+      const FseEnc& tll = S.pre.ll;
+      const FseEnc& tml = S.pre.ml;
+      const FseEnc& tof = S.pre.of;
       BitOut bo;
       bo.init(o);
       // walk the sequences backwards across segments
@@ -1086,7 +1124,15 @@ cudaError_t launch_zstd(CodecBatch b, void* scratch, cudaStream_t st)
   CHUCKY_LAUNCH(zstd_find_k, unsigned((segs + kFindWarps - 1) / kFindWarps), 32 * kFindWarps, 0, st, b, seqs, meta);
   if ((e = cudaGetLastError()) != cudaSuccess)
     return e;
-  CHUCKY_LAUNCH(zstd_block_k, unsigned(blocks), kBlockThreads, kBlockBytes + 16, st, b, seqs, meta,
+  static const PredefTables pre = [] {
+    PredefTables t{};
+    uint8_t spread[64], fill[64];
+    fse_build(t.ll, kLLNormH, 36, 6, spread, fill);
+    fse_build(t.ml, kMLNormH, 53, 6, spread, fill);
+    fse_build(t.of, kOFNormH, 29, 5, spread, fill);
+    return t;
+  }();
+  CHUCKY_LAUNCH(zstd_block_k, unsigned(blocks), kBlockThreads, kBlockBytes + 16, st, b, pre, seqs, meta,
                                                            stage, bsizes, bpc);
   if ((e = cudaGetLastError()) != cudaSuccess)
     return e;

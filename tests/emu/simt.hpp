@@ -31,6 +31,7 @@
 #define __constant__ static const
 #define __launch_bounds__(...)
 #define __restrict__
+#define __grid_constant__
 
 typedef int cudaError_t;
 typedef void* cudaStream_t;
