@@ -1,8 +1,10 @@
 // Host-only parts of the C ABI: dimension helpers, writer helpers, codec
 // predicates, crc32c, memory estimate and chunk-size advice.
+#include "kernels_codec.hpp"
 #include "plan.hpp"
 #include "stream.gpu.h"
 
+#include <algorithm>
 #include <atomic>
 #include <chrono>
 #include <cstdio>
@@ -356,7 +358,8 @@ tile_stream_gpu_memory_estimate(const tile_stream_configuration* config,
   info->chunk_pool_bytes = K * P.slot_bytes;
   const uint64_t nchunks = K * P.total_chunks;
   info->compressed_pool_bytes =
-    config->codec.id == CODEC_NONE ? 0 : nchunks * ((P.max_out + 15) / 16 * 16);
+    config->codec.id == CODEC_NONE ? 0
+                                   : 2 * nchunks * ((P.max_out + 15) / 16 * 16);
   uint64_t agg_host = 0, agg_dev = 0, shard = 0;
   for (int l = 0; l < P.nlod; ++l) {
     const chucky::LevelPlan& V = P.lv[l];
@@ -381,7 +384,17 @@ tile_stream_gpu_memory_estimate(const tile_stream_configuration* config,
     for (int l = 0; l < P.nlod; ++l)
       info->lod_bytes += P.lv[l].lod_nelem * 4;
   }
-  info->codec_bytes = nchunks * 8;
+  {
+    // encoder scratch of one wave (256 MiB of input per encoder launch)
+    const uint64_t wave = std::max<uint64_t>(
+      1, std::min<uint64_t>(nchunks, (256ull << 20) / std::max<uint64_t>(1, P.chunk_bytes)));
+    uint64_t scratch = 0;
+    if (config->codec.id == CODEC_ZSTD)
+      scratch = chucky::zstd_scratch_bytes(wave, uint32_t(P.chunk_bytes));
+    else if (config->codec.id == CODEC_LZ4_NON_STANDARD)
+      scratch = chucky::lz4_scratch_bytes(wave, uint32_t(P.chunk_bytes));
+    info->codec_bytes = 2 * nchunks * 8 + scratch;
+  }
   info->shard_bytes = shard;
   info->device_bytes = info->staging_bytes + info->chunk_pool_bytes +
                        info->compressed_pool_bytes + info->aggregate_bytes +

@@ -4,6 +4,7 @@
 #include "kernels_codec.hpp"
 #include "stream_internal.hpp"
 
+#include <algorithm>
 #include <cstdio>
 
 namespace chucky {
@@ -11,19 +12,19 @@ namespace chucky {
 int Stream::codec_init()
 {
   const uint64_t n = uint64_t(P.K) * P.total_chunks;
-  size_t bytes = 0;
-  switch (cfg.codec.id) {
-    case CODEC_NONE:
-      return 0;
-    case CODEC_LZ4_NON_STANDARD:
-      bytes = lz4_scratch_bytes(n, uint32_t(P.chunk_bytes));
-      break;
-    case CODEC_ZSTD:
-      bytes = zstd_scratch_bytes(n, uint32_t(P.chunk_bytes));
-      break;
-    default:
-      return 1;
-  }
+  if (cfg.codec.id == CODEC_NONE)
+    return 0;
+  if (cfg.codec.id != CODEC_LZ4_NON_STANDARD && cfg.codec.id != CODEC_ZSTD)
+    return 1;
+  // The encoders' scratch grows with their input; batches larger than
+  // kWaveBytes are encoded in waves that reuse one scratch area.
+  constexpr uint64_t kWaveBytes = 256ull << 20;
+  wave_chunks = std::max<uint64_t>(1, kWaveBytes / std::max<uint64_t>(1, P.chunk_bytes));
+  if (wave_chunks > n)
+    wave_chunks = n;
+  const size_t bytes = cfg.codec.id == CODEC_ZSTD
+                         ? zstd_scratch_bytes(wave_chunks, uint32_t(P.chunk_bytes))
+                         : lz4_scratch_bytes(wave_chunks, uint32_t(P.chunk_bytes));
   if (P.chunk_bytes >= (uint64_t(1) << 32))
     return 1;
   for (int i = 0; i < 2; ++i)
@@ -38,21 +39,29 @@ int Stream::codec_compress(uint64_t nchunks,
                            uint8_t* out,
                            uint64_t* sizes)
 {
-  CodecBatch b{};
-  b.in = d_pool;
-  b.in_stride = layout.chunk_stride * P.bpe;
-  b.chunk_bytes = uint32_t(P.chunk_bytes);
-  b.n_chunks = nchunks;
-  b.out = out;
-  b.out_stride = comp_stride;
-  b.out_sizes = sizes;
-  b.level = cfg.codec.level;
-  b.chunk_ids = d_ids;
-  cudaError_t e = cudaErrorInvalidValue;
-  if (cfg.codec.id == CODEC_LZ4_NON_STANDARD)
-    e = launch_lz4(b, codec_state, s_comp);
-  else if (cfg.codec.id == CODEC_ZSTD)
-    e = launch_zstd(b, codec_state, s_comp);
+  cudaError_t e = cudaSuccess;
+  for (uint64_t first = 0; first < nchunks && e == cudaSuccess;
+       first += wave_chunks) {
+    CodecBatch b{};
+    const uint64_t n = std::min<uint64_t>(wave_chunks, nchunks - first);
+    b.in_stride = layout.chunk_stride * P.bpe;
+    b.chunk_bytes = uint32_t(P.chunk_bytes);
+    b.n_chunks = n;
+    b.out_stride = comp_stride;
+    b.level = cfg.codec.level;
+    if (d_ids) { // chunk slots listed explicitly
+      b.in = d_pool;
+      b.out = out;
+      b.out_sizes = sizes;
+      b.chunk_ids = d_ids + first;
+    } else { // slots first .. first + n - 1
+      b.in = d_pool + first * b.in_stride;
+      b.out = out + first * comp_stride;
+      b.out_sizes = sizes + first;
+    }
+    e = cfg.codec.id == CODEC_ZSTD ? launch_zstd(b, codec_state, s_comp)
+                                   : launch_lz4(b, codec_state, s_comp);
+  }
   if (e != cudaSuccess) {
     std::fprintf(stderr, "chucky_gb300: %s encoder launch failed: %s\n",
                  cfg.codec.id == CODEC_ZSTD ? "zstd" : "lz4",

@@ -4,9 +4,9 @@
 // with a private hash table (12-bit hash of 4 bytes -> last position, 16-bit
 // positions relative to the segment) in shared memory.  Each step looks at
 // the 32 positions p..p+31 at once: every lane hashes the 4 bytes at its
-// position, probes the table and verifies the candidate (or takes the
-// nearest earlier lane of the same step holding the same 4 bytes, found
-// with __match_any_sync); the lowest lane
+// position, probes the table and verifies the candidate (or, for runs and
+// periods of 1, 2 or 4 bytes, the lane 1, 2 or 4 positions back in the same
+// step); the lowest lane
 // with a verified match wins (greedy, earliest match first), the warp
 // extends it 32 bytes per step, and parsing resumes after the match.  All 32
 // positions are inserted after the probe, so the table only ever holds
@@ -113,14 +113,24 @@ __device__ inline SegInfo lz77_parse_segment(const uint8_t* base,
         ok = load_u32(base, cand) == v;
       }
     }
-    // positions of this same step with equal 4 bytes are earlier
-    // candidates too (runs and short periods match on the first step)
-    const unsigned vmask = __ballot_sync(0xffffffffu, valid);
-    const unsigned peers = __match_any_sync(0xffffffffu, valid ? v : ~0u) & vmask;
-    const unsigned earlier = peers & ((1u << lane) - 1);
-    if (valid && !ok && earlier) {
-      cand = p + (31 - __clz(earlier)); // nearest earlier lane
-      ok = true;
+    // runs and short periods (1, 2, 4 bytes) match positions of this same
+    // step that are not in the table yet
+    {
+      const uint32_t v1 = __shfl_up_sync(0xffffffffu, v, 1);
+      const uint32_t v2 = __shfl_up_sync(0xffffffffu, v, 2);
+      const uint32_t v4 = __shfl_up_sync(0xffffffffu, v, 4);
+      if (valid && !ok) {
+        if (lane >= 1 && v1 == v) {
+          cand = q - 1;
+          ok = true;
+        } else if (lane >= 2 && v2 == v) {
+          cand = q - 2;
+          ok = true;
+        } else if (lane >= 4 && v4 == v) {
+          cand = q - 4;
+          ok = true;
+        }
+      }
     }
     __syncwarp();
     if (valid)

@@ -598,6 +598,7 @@ int Stream::run_epoch(uint64_t present)
       return 1;
   }
   CK(cudaEventRecord(ev_input_free[b], s_comp));
+  pending_epoch_ms.push_back(now_ms());
   in_buf ^= 1;
   in_fill = 0;
   if (accumulated >= MAX_BATCH_EPOCHS)
@@ -718,6 +719,8 @@ int Stream::kick_batch(uint32_t n_epochs, const uint32_t* epoch_masks)
   CK(cudaEventRecord(ev_batch[si], sa));
   S.busy = 1;
   S.seq = ++batch_seq;
+  S.epoch_done_ms.swap(pending_epoch_ms);
+  pending_epoch_ms.clear();
   next_slot ^= 1;
   return 0;
 }
@@ -792,7 +795,11 @@ int Stream::deliver(int si)
       S.fence[l] = io_done[l];
     }
   }
-  add_metric(metrics.sink, float(now_ms() - t0), 0, double(bytes_out));
+  const double t1 = now_ms();
+  add_metric(metrics.sink, float(t1 - t0), 0, double(bytes_out));
+  for (double e : S.epoch_done_ms)
+    latencies_ms.push_back(t1 - e);
+  S.epoch_done_ms.clear();
   return 0;
 }
 
@@ -1081,6 +1088,7 @@ tile_stream_gpu_restart(tile_stream_gpu* s, shard_sink* sink)
     I.sink = sink;
   I.cursor = 0;
   I.flushed = 0;
+  I.pending_epoch_ms.clear();
   I.accumulated = 0;
   I.in_buf = 0;
   I.in_fill = 0;
@@ -1156,4 +1164,20 @@ extern "C" uint64_t
 chucky_discard_sink_bytes(const shard_sink* s)
 {
   return reinterpret_cast<const DiscardSink*>(s)->bytes;
+}
+
+extern "C" size_t
+tile_stream_gpu_latencies(const tile_stream_gpu* s, double* out_ms, size_t cap)
+{
+  const auto& v = s->impl.latencies_ms;
+  if (out_ms)
+    for (size_t i = 0; i < v.size() && i < cap; ++i)
+      out_ms[i] = v[i];
+  return v.size();
+}
+
+extern "C" void
+tile_stream_gpu_clear_latencies(tile_stream_gpu* s)
+{
+  s->impl.latencies_ms.clear();
 }

@@ -39,6 +39,7 @@ struct DeliverySlot
   int level_of[LOD_MAX_LEVELS] = {};
   int n_levels = 0;
   io_event fence[LOD_MAX_LEVELS] = {};
+  std::vector<double> epoch_done_ms; // host time each epoch's input was in
   int busy = 0;
   uint64_t seq = 0;
 };
@@ -66,6 +67,7 @@ struct Stream
   uint64_t* d_sizes[2] = {}; // compressed sizes, one per delivery slot
   uint64_t comp_stride = 0;
   void* codec_state = nullptr;
+  uint64_t wave_chunks = 0; // chunks per encoder launch
   uint32_t* h_chunk_ids[2] = {};   // pinned staging of the encode list
   uint32_t* d_chunk_ids[2] = {};
 
@@ -109,6 +111,10 @@ struct Stream
   // shards
   Shards shards[LOD_MAX_LEVELS];
   io_event io_done[LOD_MAX_LEVELS] = {};
+
+  // append-to-delivered latency per epoch (ms)
+  std::vector<double> pending_epoch_ms; // epochs of the batch being filled
+  std::vector<double> latencies_ms;
 
   // progress
   uint64_t cursor = 0, max_cursor = 0;

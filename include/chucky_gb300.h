@@ -23,6 +23,15 @@ extern "C"
   int tile_stream_gpu_restart(struct tile_stream_gpu* s,
                               struct shard_sink* sink);
 
+  /* Append-to-delivered latency of every epoch delivered so far, in ms:
+   * from the append call that completed the epoch's input to the end of
+   * the sink writes of the batch holding it.  Writes up to `cap` values to
+   * `out_ms` (may be NULL) and returns the total count. */
+  size_t tile_stream_gpu_latencies(const struct tile_stream_gpu* s,
+                                   double* out_ms,
+                                   size_t cap);
+  void tile_stream_gpu_clear_latencies(struct tile_stream_gpu* s);
+
   /* A shard sink that discards every byte and counts them (the metering
    * sink of a throughput benchmark). */
   struct shard_sink* chucky_discard_sink_create(void);
