@@ -44,6 +44,42 @@ extern "C"
   /* crc32c (Castagnoli) of a buffer, as used by shard indexes. */
   uint32_t chucky_crc32c(const void* data, size_t len);
 
+  /* LZ4 chunk encoder that allocates no memory (no reference counterpart).
+   *
+   * For callers that must not allocate once running: an acquisition loop
+   * cannot afford cudaFree's device-wide synchronisation or an
+   * out-of-memory failure in the middle of a run.  The encoder's scratch is
+   * a fixed array of chucky_lz4_static_scratch_bytes() (32 MiB) in device
+   * memory, set up once per device by the first call made with that device
+   * current (make that first call before anything that must not see setup
+   * work).  Requests needing more scratch than that -- about 10 MiB of
+   * input per call -- are rejected.
+   *
+   * Encodes `n_chunks` chunks of `chunk_bytes` each, chunk i at
+   * d_chunks + i * in_stride (device memory, 4-byte aligned, `in_stride` a
+   * multiple of 4; the 256 bytes after the last chunk must be readable),
+   * into raw LZ4 blocks at d_out + i * out_stride (`out_stride` at least
+   * chunk_bytes + chunk_bytes / 255 + 16) and their sizes at d_sizes[i],
+   * asynchronously on `cuda_stream` (a cudaStream_t; NULL for the default
+   * stream).  The output is byte-identical to what a tile_stream_gpu with
+   * CODEC_LZ4_NON_STANDARD writes for the same chunk bytes.
+   *
+   * All calls on a device share the one scratch array: calls ordered on one
+   * CUDA stream are safe, calls that may overlap (other streams, other
+   * threads) race.  No part of the array needs to start at zero.
+   *
+   * Returns 0 on success, 1 for invalid arguments, 2 when the request
+   * exceeds the fixed scratch, 3 for a CUDA error. */
+  size_t chucky_lz4_static_scratch_bytes(void);
+  int chucky_lz4_encode_chunks_static(const void* d_chunks,
+                                      size_t chunk_bytes,
+                                      size_t in_stride,
+                                      size_t n_chunks,
+                                      void* d_out,
+                                      size_t out_stride,
+                                      uint64_t* d_sizes,
+                                      void* cuda_stream);
+
 #ifdef __cplusplus
 }
 #endif
