@@ -337,6 +337,32 @@ def run_reference(args, rank, world):
                     "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+def run_single(args):
+    """One array's stream (the u16 or the f32 cube of the workload) for
+    `--steps` untimed passes from device memory: the small case that kernel
+    profiles capture.  Prints nothing but "ok"."""
+    import torch
+    import chucky_gb300 as cg
+    lib = cg.load()
+    lib.chucky_discard_sink_create.restype = C.c_void_p
+    lib.chucky_discard_sink_destroy.argtypes = [C.c_void_p]
+    lib.tile_stream_gpu_restart.argtypes = [C.c_void_p, C.c_void_p]
+    u16, f32 = make_cubes()
+    cube = u16 if args.single == "u16" else f32
+    cfg = make_config(args.single, "mean" if args.single == "u16" else "median")
+    buf = torch.from_numpy(cube.reshape(-1).view(np.uint8)).cuda()
+    sink = lib.chucky_discard_sink_create()
+    s = cg.GpuStream(cfg, sink)
+    for _ in range(args.steps):
+        lib.tile_stream_gpu_restart(s.h, None)
+        if s.append(buf.data_ptr(), buf.numel()).error or s.flush().error:
+            raise RuntimeError("stream failed")
+    torch.cuda.synchronize()
+    s.close()
+    lib.chucky_discard_sink_destroy(sink)
+    print("ok", flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -344,7 +370,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    ap.add_argument("--single", choices=["u16", "f32"],
+                    help="profiling case: one array's stream, --steps passes, no timing")
     args = ap.parse_args()
+    if args.single:
+        return run_single(args)
     args.warmup = max(args.warmup, 3)
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

@@ -7,7 +7,8 @@
 // writes the LZ4 block format (token, literal length, literals, 16-bit
 // offset, match length; last sequence literals only; last 5 bytes literal;
 // last match starting >= 12 bytes before the end) in three passes:
-//   find : warp-parallel greedy match finding per 16 KiB segment (lz77.cuh)
+//   find : warp-parallel greedy match finding per 4 KiB segment, matches
+//          reaching back across the 16 KiB region (lz77.cuh)
 //   plan : per chunk, carry each segment's trailing literals into the next
 //          segment's first sequence and place every segment in the output
 //   emit : a warp writes its segment's sequences at that place.
@@ -49,19 +50,23 @@ struct SegMeta
   uint32_t final_ll;  // last segment: its literal count
 };
 
-__global__ void __launch_bounds__(32 * kWarps)
-lz4_find_k(CodecBatch b, Seq* seqs, SegMeta* meta)
+// One CTA per region, a warp per segment of it.
+__global__ void __launch_bounds__(32 * kSegsPerRegion)
+lz4_find_k(CodecBatch b, Seq* seqs, SegMeta* meta, uint32_t regions_per_chunk)
 {
-  __shared__ uint16_t tables[kWarps][1 << kHashLog];
+  __shared__ uint16_t tables[kSegsPerRegion][1 << kHashLog];
+  CHUCKY_DYN_SHARED(uint32_t, words); // kRegionStageWords
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const uint64_t seg = uint64_t(blockIdx.x) * kWarps + w;
-  if (seg >= b.n_chunks * b.segs_per_chunk)
-    return;
-  const uint64_t chunk = seg / b.segs_per_chunk;
-  const uint32_t k = uint32_t(seg % b.segs_per_chunk);
+  const uint64_t chunk = blockIdx.x / regions_per_chunk;
+  const uint32_t r0 = (blockIdx.x % regions_per_chunk) * kRegionBytes;
   const uint8_t* base = b.in + b.id(chunk) * b.in_stride;
   const uint32_t n = b.chunk_bytes;
-  const uint32_t s0 = k * kSegBytes;
+  const uint32_t r1 = min(n, r0 + kRegionBytes);
+  lz77_stage_region(base, r0, r1, words, threadIdx.x, blockDim.x);
+  const uint32_t s0 = r0 + w * kSegBytes;
+  if (s0 >= r1)
+    return;
+  const uint64_t seg = chunk * b.segs_per_chunk + s0 / kSegBytes;
   const uint32_t s1 = min(n, s0 + kSegBytes);
   const bool last = s1 == n;
   uint32_t start_limit = s1, match_end = s1;
@@ -72,8 +77,8 @@ lz4_find_k(CodecBatch b, Seq* seqs, SegMeta* meta)
       start_limit = s0;
   }
   Seq* out = seqs + seg * kMaxSeqPerSeg;
-  const SegInfo info =
-    lz77_parse_segment(base, s0, s1, start_limit, match_end, tables[w], out);
+  const SegInfo info = lz77_parse_segment(words, r0, s0, s1, start_limit, match_end,
+                                          tables[w], out);
   __syncwarp();
   // encoded size of everything but sequence 0's literal part
   uint32_t body = 0;
@@ -144,15 +149,6 @@ __device__ __forceinline__ uint8_t* put_len(uint8_t* o, uint32_t extra)
   }
   *o++ = uint8_t(extra);
   return o;
-}
-
-// Copy n bytes with the warp (byte per lane).
-__device__ __forceinline__ void warp_bytes(uint8_t* dst,
-                                           const uint8_t* src,
-                                           uint32_t n)
-{
-  for (uint32_t i = threadIdx.x & 31; i < n; i += 32)
-    dst[i] = src[i];
 }
 
 __global__ void __launch_bounds__(32 * kWarps)
@@ -253,6 +249,7 @@ cudaError_t launch_lz4(CodecBatch b, void* scratch, cudaStream_t st)
     return cudaSuccess;
   b.segs_per_chunk = (b.chunk_bytes + kSegBytes - 1) / kSegBytes;
   const uint64_t segs = b.n_chunks * b.segs_per_chunk;
+  const uint32_t rpc = (b.chunk_bytes + kRegionBytes - 1) / kRegionBytes;
   Seq* seqs = static_cast<Seq*>(scratch);
   // SegMeta holds a 64-bit field: start it on a 256-byte boundary
   const uintptr_t m = reinterpret_cast<uintptr_t>(seqs + segs * kMaxSeqPerSeg);
@@ -260,7 +257,8 @@ cudaError_t launch_lz4(CodecBatch b, void* scratch, cudaStream_t st)
   const unsigned grid = unsigned((segs + kWarps - 1) / kWarps);
   cudaError_t e;
   note_launches(3);
-  CHUCKY_LAUNCH(lz4_find_k, grid, 32 * kWarps, 0, st, b, seqs, meta);
+  CHUCKY_LAUNCH(lz4_find_k, unsigned(b.n_chunks * rpc), 32 * kSegsPerRegion,
+                kRegionStageWords * sizeof(uint32_t), st, b, seqs, meta, rpc);
   if ((e = cudaGetLastError()) != cudaSuccess)
     return e;
   CHUCKY_LAUNCH(lz4_plan_k, unsigned((b.n_chunks + 127) / 128), 128, 0, st, b, meta);

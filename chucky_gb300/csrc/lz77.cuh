@@ -1,17 +1,27 @@
 // Warp-parallel greedy LZ77 match finder shared by the LZ4 and zstd encoders.
 //
-// A chunk is cut into segments of kSegBytes; one warp parses one segment
-// with a private hash table (12-bit hash of 4 bytes -> last position, 16-bit
-// positions relative to the segment) in shared memory.  Each step looks at
-// the 32 positions p..p+31 at once: every lane hashes the 4 bytes at its
-// position, probes the table and verifies the candidate (or, for runs and
-// periods of 1, 2 or 4 bytes, the lane 1, 2 or 4 positions back in the same
-// step); the lowest lane
-// with a verified match wins (greedy, earliest match first), the warp
-// extends it 32 bytes per step, and parsing resumes after the match.  All 32
-// positions are inserted after the probe, so the table only ever holds
-// earlier positions.  Matches stay inside the segment, so segments are
-// independent and the parse is deterministic.
+// A chunk is cut into regions of kRegionBytes and each region into segments
+// of kSegBytes.  One CTA of kSegsPerRegion warps takes one region: all its
+// threads stage the region's bytes in shared memory (lz77_stage_region),
+// then warp w parses segment w of the region with a private hash table
+// (kHashLog-bit hash of 4 bytes -> last position, 16-bit positions relative
+// to the region).  Before parsing, a warp enters every position of the
+// region that precedes its segment into its table (insert only), so its
+// matches may reach back to the start of the region, as a single parse of
+// the region would; the segments are parsed side by side.
+//
+// The segment is scanned in windows of 32 positions, one per lane.  Every
+// lane hashes the 4 bytes at its position, probes the table, verifies the
+// candidate (or, for runs and periods of 1, 2 or 4 bytes, the lane 1, 2 or
+// 4 positions back in the same window) and measures the match on its own,
+// up to kLaneExtend bytes; then all 32 positions enter the table.  The
+// greedy parse then takes, within the window, the lowest position at or
+// after the parse point with a match of at least `min_match` bytes, as many
+// times as the window allows; a match that reaches kLaneExtend bytes is
+// extended by the whole warp, 32 bytes per step.  Windows inside a long
+// match are skipped.  Matches end inside their segment and start inside
+// their region.  (When lanes of one window share a hash slot the hardware
+// keeps one of their stores.)
 //
 // Output per segment: sequences (literal length, match length, offset) in
 // scratch, the sequence count and the trailing literal count.
@@ -21,10 +31,20 @@
 
 namespace chucky {
 
-constexpr int kSegLog = 14;
-constexpr uint32_t kSegBytes = 1u << kSegLog; // 16 KiB
-constexpr int kHashLog = 12;
+constexpr int kSegLog = 12;
+constexpr uint32_t kSegBytes = 1u << kSegLog; // 4 KiB: one warp's parse
+constexpr int kRegionLog = 14;
+constexpr uint32_t kRegionBytes = 1u << kRegionLog; // 16 KiB: match window
+constexpr uint32_t kSegsPerRegion = kRegionBytes / kSegBytes;
+constexpr int kHashLog = 10;
 constexpr uint32_t kMaxSeqPerSeg = kSegBytes / 4 + 1;
+// 32-bit words of a staged region: the region plus a spare vector for reads
+// that straddle its end.
+constexpr uint32_t kRegionStageWords = kRegionBytes / 4 + 4;
+// bytes a lane measures of its own match before the warp takes over
+constexpr uint32_t kLaneExtend = 64;
+static_assert((2u << kHashLog) >= kSegBytes / 8,
+              "a warp's table holds its literal bitmap");
 
 struct Seq
 {
@@ -39,13 +59,10 @@ struct SegInfo
   uint32_t trailing; // literals after the last match of the segment
 };
 
-// 4 bytes at an arbitrary byte position of a 4-byte aligned buffer; the
-// buffer must stay readable 4 bytes past `pos + 3`.
-__device__ __forceinline__ uint32_t load_u32(const uint8_t* base, uint32_t pos)
+// 4 bytes at byte position `pos` of a word array.
+__device__ __forceinline__ uint32_t word_at(const uint32_t* w, uint32_t pos)
 {
-  const uint32_t* w = reinterpret_cast<const uint32_t*>(base) + (pos >> 2);
-  const uint32_t lo = __ldg(w), hi = __ldg(w + 1);
-  return __funnelshift_r(lo, hi, (pos & 3) * 8);
+  return __funnelshift_r(w[pos >> 2], w[(pos >> 2) + 1], (pos & 3) * 8);
 }
 
 __device__ __forceinline__ uint32_t hash4(uint32_t v)
@@ -53,11 +70,42 @@ __device__ __forceinline__ uint32_t hash4(uint32_t v)
   return (v * 2654435761u) >> (32 - kHashLog);
 }
 
-// Parse segment [s0, s1) of a chunk at `base` (4-byte aligned).  Matches
-// may start before `start_limit` and end at or before `match_end`; bytes
-// from `s0` on are visible to the matcher.  `table` holds 1 << kHashLog
-// u16 entries private to this warp.
-__device__ inline SegInfo lz77_parse_segment(const uint8_t* base,
+// Copy bytes [r0, r1) of a chunk at `base` (4-byte aligned; r0 a multiple
+// of 16; readable 16 bytes past r1) into `words` (kRegionStageWords words of
+// shared memory) with all `nthreads` threads of the CTA; ends with a CTA
+// barrier.
+__device__ __forceinline__ void lz77_stage_region(const uint8_t* base,
+                                                  uint32_t r0,
+                                                  uint32_t r1,
+                                                  uint32_t* words,
+                                                  unsigned tid,
+                                                  unsigned nthreads)
+{
+  const uint8_t* src = base + r0;
+  const uint32_t nvec = (r1 - r0 + 15) >> 4;
+  if ((reinterpret_cast<uintptr_t>(src) & 15) == 0) {
+    const uint4* v = reinterpret_cast<const uint4*>(src);
+    uint4* d = reinterpret_cast<uint4*>(words);
+#pragma unroll 4
+    for (uint32_t i = tid; i < nvec; i += nthreads)
+      d[i] = __ldg(v + i);
+  } else {
+    const uint32_t* v = reinterpret_cast<const uint32_t*>(src);
+#pragma unroll 8
+    for (uint32_t i = tid; i < 4 * nvec; i += nthreads)
+      words[i] = __ldg(v + i);
+  }
+  if (tid < 4)
+    words[4 * nvec + tid] = 0;
+  __syncthreads();
+}
+
+// Parse segment [s0, s1) of a chunk whose bytes from r0 (the region start,
+// r0 <= s0) on are staged in `words`.  Matches may start at positions in
+// [s0, start_limit), reach back to r0 and end at or before `match_end`.
+// `table` holds 1 << kHashLog u16 entries private to this warp.
+__device__ inline SegInfo lz77_parse_segment(const uint32_t* words,
+                                             uint32_t r0,
                                              uint32_t s0,
                                              uint32_t s1,
                                              uint32_t start_limit,
@@ -67,54 +115,41 @@ __device__ inline SegInfo lz77_parse_segment(const uint8_t* base,
                                              uint32_t min_match = 4)
 {
   const int lane = threadIdx.x & 31;
+  const uint8_t* bytes = reinterpret_cast<const uint8_t*>(words);
   for (int i = lane; i < (1 << kHashLog); i += 32)
     table[i] = 0xFFFF;
   __syncwarp();
-  // The bytes under the 32 probed positions come from a 256-byte window
-  // held in registers (lane i: words i and 32+i), refilled with coalesced
-  // 128-byte warp loads, so probing costs no memory latency.
-  const uint32_t* wbase = reinterpret_cast<const uint32_t*>(base);
-  uint32_t win = s0 & ~3u; // byte position of the window start
-  uint32_t cur = __ldg(wbase + (win >> 2) + lane);
-  uint32_t nxt = __ldg(wbase + (win >> 2) + 32 + lane);
-  uint32_t p = s0, lit_start = s0, nseq = 0;
-  while (p < start_limit) {
-    if (p >= win + 128) { // slide (or jump) the window
-      if (p < win + 256) {
-        cur = nxt;
-        win += 128;
-        nxt = __ldg(wbase + (win >> 2) + 32 + lane);
-      } else {
-        win = p & ~3u;
-        cur = __ldg(wbase + (win >> 2) + lane);
-        nxt = __ldg(wbase + (win >> 2) + 32 + lane);
-      }
-    }
-    const uint32_t q = p + lane;
-    const bool valid = q < start_limit && q + 4 <= match_end;
-    // words j and j+1 of the window hold bytes [q, q+4)
-    const uint32_t j = (q - win) >> 2; // <= 63 - 1 since p < win + 128
-    const uint32_t a0 = __shfl_sync(0xffffffffu, cur, j & 31);
-    const uint32_t b0 = __shfl_sync(0xffffffffu, nxt, j & 31);
-    const uint32_t a1 = __shfl_sync(0xffffffffu, cur, (j + 1) & 31);
-    const uint32_t b1 = __shfl_sync(0xffffffffu, nxt, (j + 1) & 31);
-    const uint32_t lo = j < 32 ? a0 : b0;
-    const uint32_t hi = (j + 1) < 32 ? a1 : b1;
-    uint32_t v = 0, h = 0, cand = 0xFFFFFFFFu;
+  // positions below are relative to r0
+  const uint32_t first = s0 - r0;
+  const uint32_t lim = start_limit > s0 ? start_limit - r0 : first;
+  const uint32_t end = match_end - r0;
+  // history: the region's positions before this segment
+  for (uint32_t w0 = 0; w0 < first; w0 += 32) {
+    const uint32_t q = w0 + lane;
+    const uint32_t h = hash4(word_at(words, q));
+    __syncwarp();
+    table[h] = uint16_t(q);
+  }
+  __syncwarp();
+  uint32_t w0 = first, p = first, lit_start = first, nseq = 0;
+  while (w0 < lim) {
+    const uint32_t q = w0 + lane;
+    const bool valid = q < lim && q + 4 <= end;
+    uint32_t v = 0, h = 0, cand = 0;
     bool ok = false;
     if (valid) {
-      v = __funnelshift_r(lo, hi, (q & 3) * 8);
+      v = word_at(words, q);
       h = hash4(v);
       const uint16_t t = table[h];
-      // entries can be ahead of q: positions probed in an earlier step
-      // may lie past where the last match ended
-      if (t != 0xFFFF && s0 + t < q) {
-        cand = s0 + t;
-        ok = load_u32(base, cand) == v;
+      // entries can be ahead of q: a window skipped into a long match
+      // leaves later positions in the table
+      if (t != 0xFFFF && t < q) {
+        cand = t;
+        ok = word_at(words, cand) == v;
       }
     }
     // runs and short periods (1, 2, 4 bytes) match positions of this same
-    // step that are not in the table yet
+    // window that are not in the table yet
     {
       const uint32_t v1 = __shfl_up_sync(0xffffffffu, v, 1);
       const uint32_t v2 = __shfl_up_sync(0xffffffffu, v, 2);
@@ -132,43 +167,164 @@ __device__ inline SegInfo lz77_parse_segment(const uint8_t* base,
         }
       }
     }
+    // this lane's match length, up to kLaneExtend bytes
+    uint32_t len = 0;
+    if (ok) {
+      len = 4;
+      while (len < kLaneExtend) {
+        if (q + len + 4 > end) { // the last bytes before `end`, one by one
+          while (q + len < end && bytes[q + len] == bytes[cand + len])
+            ++len;
+          break;
+        }
+        const uint32_t x = word_at(words, q + len) ^ word_at(words, cand + len);
+        if (x) {
+          len += uint32_t(__ffs(int(x)) - 1) >> 3;
+          break;
+        }
+        len += 4;
+      }
+    }
     __syncwarp();
     if (valid)
-      table[h] = uint16_t(q - s0);
+      table[h] = uint16_t(q);
     __syncwarp();
-    const unsigned hit = __ballot_sync(0xffffffffu, ok);
-    if (!hit) {
-      p += 32;
-      continue;
-    }
-    const int k = __ffs(hit) - 1;
-    const uint32_t mpos = __shfl_sync(0xffffffffu, q, k);
-    const uint32_t src = __shfl_sync(0xffffffffu, cand, k);
-    // extend 32 bytes per step
-    uint32_t len = 4;
+    unsigned hits = __ballot_sync(0xffffffffu, ok && len >= min_match);
+    // greedy parse through this window
     for (;;) {
-      const uint32_t a = mpos + len + lane, b = src + len + lane;
-      const bool same = a < match_end && base[a] == base[b];
-      const unsigned eq = __ballot_sync(0xffffffffu, same);
-      if (eq == 0xffffffffu) {
-        len += 32;
-        continue;
+      const uint32_t from = p > w0 ? p - w0 : 0;
+      if (from >= 32)
+        break;
+      const unsigned m = hits & (0xffffffffu << from);
+      if (!m)
+        break;
+      const int k = __ffs(int(m)) - 1;
+      const uint32_t mpos = w0 + k;
+      const uint32_t src = __shfl_sync(0xffffffffu, cand, k);
+      uint32_t mlen = __shfl_sync(0xffffffffu, len, k);
+      if (mlen >= kLaneExtend) { // long match: the warp extends it
+        for (;;) {
+          const uint32_t a = mpos + mlen + lane, b = src + mlen + lane;
+          const bool same = a < end && bytes[a] == bytes[b];
+          const unsigned eq = __ballot_sync(0xffffffffu, same);
+          if (eq == 0xffffffffu) {
+            mlen += 32;
+            continue;
+          }
+          mlen += __ffs(int(~eq)) - 1;
+          break;
+        }
       }
-      len += __ffs(~eq) - 1;
-      break;
+      if (lane == 0)
+        out[nseq] = Seq{ mpos - lit_start, mlen, mpos - src };
+      ++nseq;
+      p = mpos + mlen;
+      lit_start = p;
     }
-    if (len < min_match) { // too short to pay for a sequence: literals
-      p = mpos + 1;
-      continue;
-    }
-    if (lane == 0)
-      out[nseq] = Seq{ mpos - lit_start, len, mpos - src };
-    ++nseq;
-    p = mpos + len;
-    lit_start = p;
+    // next window; skip windows that lie inside a long match
+    w0 = p >= w0 + 64 ? p : w0 + 32;
   }
   __syncwarp();
-  return SegInfo{ nseq, s1 - lit_start };
+  return SegInfo{ nseq, (s1 - r0) - lit_start };
+}
+
+// Literal bytes of a parsed segment (those its matches do not cover), in
+// order, compacted in place to the start of the segment's bytes in the
+// staged region; returns their count.  Call after every warp of the CTA
+// has finished parsing (the region is no longer read as history).
+// `bitmap` is kSegBytes / 8 bytes of the warp's (free again) hash table.
+// `hist` (256 counts, zeroed) receives the literal bytes when not null.
+__device__ inline uint32_t lz77_compact_literals(uint32_t* words,
+                                                 uint32_t r0,
+                                                 uint32_t s0,
+                                                 uint32_t s1,
+                                                 const Seq* sq,
+                                                 uint32_t nseq,
+                                                 uint32_t* bitmap,
+                                                 uint32_t* hist)
+{
+  const unsigned lane = threadIdx.x & 31;
+  const uint32_t n = s1 - s0;
+  const uint32_t nwords = (n + 31) >> 5;
+  // bit i of word j: position 32 j + i is a literal
+  for (uint32_t j = lane; j < nwords; j += 32) {
+    const uint32_t lo = 32 * j;
+    bitmap[j] = n - lo >= 32 ? 0xFFFFFFFFu : (1u << (n - lo)) - 1;
+  }
+  __syncwarp();
+  // clear the bits under every match
+  uint32_t pos = 0;
+  for (uint32_t base = 0; base < nseq; base += 32) {
+    const uint32_t i = base + lane;
+    uint32_t lt = 0, ml = 0;
+    if (i < nseq) {
+      const Seq q = sq[i];
+      lt = q.lit;
+      ml = q.match;
+    }
+    uint32_t ex = lt + ml;
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, ex, o);
+      if (lane >= o)
+        ex += y;
+    }
+    const uint32_t tot = __shfl_sync(0xffffffffu, ex, 31);
+    ex -= lt + ml;
+    uint32_t a = pos + ex + lt; // match start, segment-relative
+    const uint32_t e = a + ml;
+    while (a < e) {
+      const uint32_t j = a >> 5, b = a & 31;
+      const uint32_t k = min(32u - b, e - a);
+      const uint32_t mask = (k == 32 ? 0xFFFFFFFFu : ((1u << k) - 1)) << b;
+      if (mask == 0xFFFFFFFFu)
+        bitmap[j] = 0;
+      else
+        atomicAnd(bitmap + j, ~mask);
+      a += k;
+    }
+    pos += tot;
+  }
+  __syncwarp();
+  // compact 1 KiB at a time: every lane reads its 32 bytes into registers,
+  // then writes their literal bytes at the final place (never after the
+  // source, so later bytes are still intact)
+  uint8_t* bytes = reinterpret_cast<uint8_t*>(words) + (s0 - r0);
+  uint32_t out = 0;
+  for (uint32_t c = 0; c < nwords; c += 32) {
+    const uint32_t j = c + lane;
+    uint32_t m = 0;
+    uint4 lo4 = make_uint4(0, 0, 0, 0), hi4 = make_uint4(0, 0, 0, 0);
+    if (j < nwords) {
+      m = bitmap[j];
+      const uint4* src = reinterpret_cast<const uint4*>(bytes + 32 * j);
+      lo4 = src[0];
+      hi4 = src[1];
+    }
+    const uint32_t cnt = __popc(m);
+    uint32_t ex = cnt;
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, ex, o);
+      if (lane >= o)
+        ex += y;
+    }
+    const uint32_t tot = __shfl_sync(0xffffffffu, ex, 31);
+    ex -= cnt;
+    __syncwarp();
+    uint32_t d = out + ex;
+    while (m) {
+      const int i = __ffs(int(m)) - 1;
+      m &= m - 1;
+      const uint32_t wd = i < 16 ? (i < 8 ? (i < 4 ? lo4.x : lo4.y) : (i < 12 ? lo4.z : lo4.w))
+                                 : (i < 24 ? (i < 20 ? hi4.x : hi4.y) : (i < 28 ? hi4.z : hi4.w));
+      const uint8_t c8 = uint8_t(wd >> ((i & 3) * 8));
+      bytes[d++] = c8;
+      if (hist)
+        atomicAdd(hist + c8, 1u);
+    }
+    out += tot;
+    __syncwarp();
+  }
+  return out;
 }
 
 } // namespace chucky

@@ -23,6 +23,7 @@
 #include "stream_internal.hpp"
 
 #include <algorithm>
+#include <atomic>
 #include <cstddef>
 #include <chrono>
 #include <cstdio>
@@ -1119,14 +1120,15 @@ struct DiscardSink
 {
   shard_sink base;
   shard_writer w;
-  uint64_t bytes;
+  std::atomic<uint64_t> bytes; // one sink may serve streams on several threads
 };
 
 int discard_write(shard_writer* self, uint64_t, const void* b, const void* e)
 {
   DiscardSink* d = reinterpret_cast<DiscardSink*>(
     reinterpret_cast<char*>(self) - offsetof(DiscardSink, w));
-  d->bytes += uint64_t(static_cast<const char*>(e) - static_cast<const char*>(b));
+  d->bytes.fetch_add(uint64_t(static_cast<const char*>(e) - static_cast<const char*>(b)),
+                     std::memory_order_relaxed);
   return 0;
 }
 
@@ -1163,7 +1165,7 @@ chucky_discard_sink_destroy(shard_sink* s)
 extern "C" uint64_t
 chucky_discard_sink_bytes(const shard_sink* s)
 {
-  return reinterpret_cast<const DiscardSink*>(s)->bytes;
+  return reinterpret_cast<const DiscardSink*>(s)->bytes.load();
 }
 
 extern "C" size_t

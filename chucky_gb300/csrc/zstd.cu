@@ -33,10 +33,10 @@ constexpr uint32_t kBlockLog = 15;
 constexpr uint32_t kBlockBytes = 1u << kBlockLog; // 32 KiB
 constexpr uint32_t kSegsPerBlock = kBlockBytes / kSegBytes;
 constexpr uint32_t kStageBytes = kBlockBytes + 1024;
-constexpr int kStreamThreads = 32;                // a warp per Huffman stream
+constexpr int kStreamThreads = 64;                // two warps per Huffman stream
 constexpr int kBlockThreads = 4 * kStreamThreads; // >= a warp per segment
 static_assert(kBlockThreads >= 32 * int(kSegsPerBlock), "warp per segment");
-constexpr int kFindWarps = 4;
+static_assert(kStreamThreads % 32 == 0, "whole warps per stream");
 constexpr uint32_t kHufMaxBits = 11;
 #ifndef CHUCKY_ZSTD_MIN_MATCH
 #define CHUCKY_ZSTD_MIN_MATCH 6
@@ -47,6 +47,9 @@ constexpr uint32_t kMinMatch = CHUCKY_ZSTD_MIN_MATCH;
 struct ZSeg
 {
   uint32_t nseq, trailing, matched; // matched = bytes covered by matches
+  // bits 0-7 first literal byte, bit 8 every literal equals it (or none);
+  // bits 16-23 first input byte, bit 24 every input byte equals it
+  uint32_t flags;
 };
 
 // ---------------------------------------------------------------------------
@@ -204,60 +207,81 @@ __constant__ uint8_t kMLBits[53] = { 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0,
                                      0, 0, 0, 0, 1, 1, 1, 1, 2, 2, 3, 3, 4, 4,
                                      5, 7, 8, 9, 10, 11, 12, 13, 14, 15, 16 };
 
-__device__ __forceinline__ int ll_code(uint32_t ll)
-{
-  if (ll < 16)
-    return int(ll);
-  if (ll >= 64)
-    return highbit(ll) + 19;
-  // 16..63
-  int c = 16;
-  while (c < 35 && kLLBase[c + 1] <= ll)
-    ++c;
-  return c;
-}
-
-__device__ __forceinline__ int ml_code(uint32_t ml)
-{
-  const uint32_t mb = ml - 3;
-  if (mb < 32)
-    return int(mb);
-  if (mb >= 128)
-    return highbit(mb) + 36;
-  int c = 32;
-  while (c < 52 && kMLBase[c + 1] <= ml)
-    ++c;
-  return c;
-}
-
 // ---------------------------------------------------------------------------
 // find
 // ---------------------------------------------------------------------------
 
-__global__ void __launch_bounds__(32 * kFindWarps)
-zstd_find_k(CodecBatch b, Seq* seqs, ZSeg* meta)
+// One CTA per region, a warp per segment.  Besides the sequences, every
+// segment leaves its literal bytes, compacted, in its slot of `litbuf`
+// (kSegBytes each), adds them to its chunk's literal histogram
+// (`chunk_hist`, 256 counts per chunk, zeroed before the launch) and
+// records whether its input and its literals are single-valued.
+__global__ void __launch_bounds__(32 * kSegsPerRegion)
+zstd_find_k(CodecBatch b,
+            Seq* seqs,
+            ZSeg* meta,
+            uint32_t* chunk_hist,
+            uint8_t* litbuf,
+            uint32_t regions_per_chunk)
 {
-  __shared__ uint16_t tables[kFindWarps][1 << kHashLog];
+  __shared__ uint16_t tables[kSegsPerRegion][1 << kHashLog];
+  CHUCKY_DYN_SHARED(uint32_t, words); // kRegionStageWords
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const uint64_t seg = uint64_t(blockIdx.x) * kFindWarps + w;
-  if (seg >= b.n_chunks * b.segs_per_chunk)
-    return;
-  const uint64_t chunk = seg / b.segs_per_chunk;
-  const uint32_t k = uint32_t(seg % b.segs_per_chunk);
+  const uint64_t chunk = blockIdx.x / regions_per_chunk;
+  const uint32_t r0 = (blockIdx.x % regions_per_chunk) * kRegionBytes;
   const uint8_t* base = b.in + b.id(chunk) * b.in_stride;
-  const uint32_t s0 = k * kSegBytes;
-  const uint32_t s1 = min(b.chunk_bytes, s0 + kSegBytes);
-  Seq* out = seqs + seg * kMaxSeqPerSeg;
-  const SegInfo info =
-    lz77_parse_segment(base, s0, s1, s1, s1, tables[w], out, kMinMatch);
-  __syncwarp();
+  const uint32_t r1 = min(b.chunk_bytes, r0 + kRegionBytes);
+  lz77_stage_region(base, r0, r1, words, threadIdx.x, blockDim.x);
+  const uint32_t s0 = r0 + w * kSegBytes;
+  const bool has = s0 < r1;
+  const uint32_t s1 = has ? min(r1, s0 + kSegBytes) : s0;
+  const uint64_t seg = chunk * b.segs_per_chunk + s0 / kSegBytes;
+  Seq* out = seqs + (has ? seg : 0) * kMaxSeqPerSeg;
+  SegInfo info{ 0, 0 };
+  if (has)
+    info = lz77_parse_segment(words, r0, s0, s1, s1, s1, tables[w], out, kMinMatch);
+  __syncthreads(); // the region is no longer needed as history
+  if (!has)
+    return;
   uint32_t matched = 0;
   for (uint32_t i = lane; i < info.nseq; i += 32)
     matched += out[i].match;
   for (int o = 16; o; o >>= 1)
     matched += __shfl_xor_sync(0xffffffffu, matched, o);
+  // single-valued input?
+  const uint8_t* sb = reinterpret_cast<const uint8_t*>(words) + (s0 - r0);
+  const uint32_t n = s1 - s0;
+  const uint8_t in0 = sb[0];
+  bool same = true;
+  for (uint32_t i = lane; i < n; i += 32)
+    same &= sb[i] == in0;
+  const bool in_same = __all_sync(0xffffffffu, same);
+  // literals: compacted in place, counted, copied out
+  uint32_t* bitmap = reinterpret_cast<uint32_t*>(tables[w]);
+  uint32_t* hist = bitmap + (kSegBytes / 32 + 31) / 32 * 32; // after the bitmap
+  for (int i = lane; i < 256; i += 32)
+    hist[i] = 0;
+  __syncwarp();
+  const uint32_t nlit =
+    lz77_compact_literals(words, r0, s0, s1, out, info.nseq, bitmap, hist);
+  const uint8_t lit0 = nlit ? sb[0] : 0;
+  same = true;
+  for (uint32_t i = lane; i < nlit; i += 32)
+    same &= sb[i] == lit0;
+  const bool lit_same = __all_sync(0xffffffffu, same);
+  const uint4* src = reinterpret_cast<const uint4*>(sb);
+  uint4* dst = reinterpret_cast<uint4*>(litbuf + seg * kSegBytes);
+  for (uint32_t i = lane; i < (nlit + 15) / 16; i += 32)
+    dst[i] = src[i];
+  __syncwarp();
+  uint32_t* ch = chunk_hist + chunk * 256;
+  for (int i = lane; i < 256; i += 32)
+    if (hist[i])
+      atomicAdd(ch + i, hist[i]);
   if (lane == 0)
-    meta[seg] = ZSeg{ info.nseq, info.trailing, matched };
+    meta[seg] = ZSeg{ info.nseq, info.trailing, matched,
+                      uint32_t(lit0) | (lit_same ? 1u << 8 : 0u) |
+                        (uint32_t(in0) << 16) | (in_same ? 1u << 24 : 0u) };
 }
 
 // ---------------------------------------------------------------------------
@@ -565,17 +589,33 @@ __device__ bool huff_describe(Huff& h, HuffScratch& x, FseEnc& t)
 // block
 // ---------------------------------------------------------------------------
 
-struct BlockShared
+// Huffman table of a chunk's literals, built once per chunk
+// (zstd_table_k) and used by every block of the chunk.
+struct ChunkTable
+{
+  uint32_t cl[256];    // code | length << 16; 0 for absent symbols
+  uint8_t desc[320];   // tree description (header byte + payload)
+  uint32_t desc_len;
+  uint32_t ok;         // a usable table exists
+};
+
+struct TableShared
 {
   uint32_t hist[256];
-  uint32_t whist[kSegsPerBlock][256]; // per-warp histograms (merged)
-  uint16_t sorted[256];               // used symbols by (count, symbol)
+  uint16_t sorted[256]; // used symbols by (count, symbol)
   uint32_t nsym;
-  PredefTables pre;                   // predefined sequence tables
-  FseEnc tw;                          // Huffman weights table
+  uint32_t ok;
+  FseEnc tw;            // Huffman weights table
   HuffScratch hx;
   Huff huff;
+};
+
+struct BlockShared
+{
+  uint32_t cl[256];                   // the chunk's Huffman codes
+  PredefTables pre;                   // predefined sequence tables
   uint32_t seg_nseq[kSegsPerBlock];
+  uint32_t seg_seq0[kSegsPerBlock];   // block index of the segment's first sequence
   uint32_t seg_carry[kSegsPerBlock];
   uint32_t seg_litout[kSegsPerBlock]; // literal buffer offset of seg start
   uint32_t nseq, nlit;
@@ -584,13 +624,154 @@ struct BlockShared
   uint32_t lit_mode;      // 0 raw, 1 rle, 2 huffman
   uint32_t lit_hdr;       // literals section header bytes
   uint32_t lit_size;      // literals section bytes (header included)
+  uint32_t lit_same;      // every literal equals the first
   uint32_t all_same;
+  // sequences section
+  uint32_t ll_base[36], ml_base[53];
+  uint8_t ll_bits[36], ml_bits[53];
+  uint32_t final_state[3];    // LL, ML, OF states after the last step
+  uint32_t warp_bits[kBlockThreads / 32];
+  uint32_t seq_bad;
+  uint32_t seq_csize;         // compressed block bytes (after the header)
 };
 
 __device__ __forceinline__ void put_le(uint8_t* p, uint64_t v, int n)
 {
   for (int i = 0; i < n; ++i)
     p[i] = uint8_t(v >> (8 * i));
+}
+
+// Bit packing into a stream shared by many threads: each thread owns a
+// contiguous bit range [start, start + n) of the stream at `p` (zeroed
+// beforehand).  Words wholly inside the range are stored plainly; the first
+// (shared with the bytes or thread before) and the last are OR-ed in.
+struct BitPack
+{
+  uint32_t* w;
+  uint64_t acc, word;
+  int fill;
+  bool first;
+  __device__ void init(uint8_t* p, uint32_t start_bit)
+  {
+    w = reinterpret_cast<uint32_t*>(reinterpret_cast<uintptr_t>(p) & ~uintptr_t(3));
+    const uint64_t pos = uint64_t(reinterpret_cast<uintptr_t>(p) & 3) * 8 + start_bit;
+    word = pos >> 5;
+    fill = int(pos & 31);
+    first = fill != 0;
+    acc = 0;
+  }
+  // n <= 32
+  __device__ __forceinline__ void put(uint32_t v, int n)
+  {
+    acc |= (uint64_t(v) & ((uint64_t(1) << n) - 1)) << fill;
+    fill += n;
+    if (fill >= 32) {
+      if (first)
+        atomicOr(w + word, uint32_t(acc));
+      else
+        w[word] = uint32_t(acc);
+      first = false;
+      acc >>= 32;
+      fill -= 32;
+      ++word;
+    }
+  }
+  __device__ void flush()
+  {
+    if (fill > 0)
+      atomicOr(w + word, uint32_t(acc));
+  }
+};
+
+__device__ __forceinline__ int ll_code_s(uint32_t ll, const uint32_t* base)
+{
+  if (ll < 16)
+    return int(ll);
+  if (ll >= 64)
+    return highbit(ll) + 19;
+  int c = 16; // 16..63
+  while (c < 35 && base[c + 1] <= ll)
+    ++c;
+  return c;
+}
+
+__device__ __forceinline__ int ml_code_s(uint32_t ml, const uint32_t* base)
+{
+  const uint32_t mb = ml - 3;
+  if (mb < 32)
+    return int(mb);
+  if (mb >= 128)
+    return highbit(mb) + 36;
+  int c = 32;
+  while (c < 52 && base[c + 1] <= ml)
+    ++c;
+  return c;
+}
+
+// Literal length (with the carry into a segment's first sequence), match
+// length and offset value (offset + 3, no repeat offsets) of block
+// sequence j.
+__device__ __forceinline__ void seq_at(const BlockShared& S,
+                                       const Seq* seqs,
+                                       uint64_t segbase,
+                                       uint32_t nsegs,
+                                       uint32_t j,
+                                       uint32_t& ll,
+                                       uint32_t& ml,
+                                       uint32_t& off)
+{
+  uint32_t k = 0;
+  while (k + 1 < nsegs && j >= S.seg_seq0[k + 1])
+    ++k;
+  const uint32_t i = j - S.seg_seq0[k];
+  const Seq q = seqs[(segbase + k) * kMaxSeqPerSeg + i];
+  ll = q.lit + (i == 0 ? S.seg_carry[k] : 0);
+  ml = q.match;
+  off = q.offset + 3;
+}
+
+// Low bits of FSE state u (v = u + table size) when encoding `sym`.
+template<typename F>
+__device__ __forceinline__ int state_bits(const FseEnc& t, uint32_t u, int sym, F& put)
+{
+  const uint32_t v = u + (1u << t.al);
+  const int c = t.count[sym];
+  int nb = t.al - highbit(uint32_t(c));
+  if ((v >> nb) < uint32_t(c))
+    --nb;
+  put(v, nb);
+  return nb;
+}
+
+// Bits of block sequence j in stream order (RFC 8878 3.1.1.3.2.1): for all
+// but the block's last sequence (the stream's first) the OF, ML and LL
+// state bits, then the LL, ML and OF extra bits.  `st` holds the state each
+// sequence starts from ([3][nseq]: LL, ML, OF).  Returns the bit count.
+template<typename F>
+__device__ __forceinline__ uint32_t seq_emit(const BlockShared& S,
+                                             const Seq* seqs,
+                                             uint64_t segbase,
+                                             uint32_t nsegs,
+                                             uint32_t nseq,
+                                             const uint8_t* st,
+                                             uint32_t j,
+                                             F&& put)
+{
+  uint32_t ll, ml, off;
+  seq_at(S, seqs, segbase, nsegs, j, ll, ml, off);
+  const int lc = ll_code_s(ll, S.ll_base), mc = ml_code_s(ml, S.ml_base);
+  const int oc = highbit(off);
+  uint32_t bits = 0;
+  if (j + 1 < nseq) {
+    bits += state_bits(S.pre.of, st[2 * nseq + j], oc, put);
+    bits += state_bits(S.pre.ml, st[nseq + j], mc, put);
+    bits += state_bits(S.pre.ll, st[j], lc, put);
+  }
+  const int lb = S.ll_bits[lc], mb = S.ml_bits[mc];
+  put(ll - S.ll_base[lc], lb);
+  put(ml - S.ml_base[mc], mb);
+  put(off - (1u << oc), oc);
+  return bits + lb + mb + oc;
 }
 
 // Visit lits[hi-1], lits[hi-2], ..., lits[lo] (descending), reading the
@@ -615,38 +796,54 @@ __device__ __forceinline__ void for_each_desc(const uint8_t* lits,
   }
 }
 
-// Copy n literal bytes in[src..) -> lits[dst..) with one warp and count them
-// in `hist`; the body moves whole aligned 32-bit words of the input.
-__device__ __forceinline__ void gather_run(const uint8_t* in,
-                                           uint32_t src,
-                                           uint32_t n,
-                                           uint8_t* lits,
-                                           uint32_t dst,
-                                           uint32_t* hist,
-                                           unsigned lane)
+// One CTA per chunk: the length-limited Huffman code of the chunk's
+// literal histogram and its tree description (thread 0 builds, the rest
+// rank the symbols and publish the table).
+__global__ void __launch_bounds__(kBlockThreads)
+zstd_table_k(const uint32_t* chunk_hist, ChunkTable* tables)
 {
-  const uint32_t lead = (4 - (src & 3)) & 3;
-  const uint32_t h = n < lead ? n : lead;
-  if (lane < h) {
-    const uint8_t c = in[src + lane];
-    lits[dst + lane] = c;
-    atomicAdd(&hist[c], 1u);
-  }
-  const uint32_t nw = (n - h) >> 2;
-  const uint32_t* w = reinterpret_cast<const uint32_t*>(in + src + h);
-  for (uint32_t i = lane; i < nw; i += 32) {
-    const uint32_t v = w[i];
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      const uint8_t c = uint8_t(v >> (8 * k));
-      lits[dst + h + 4 * i + k] = c;
-      atomicAdd(&hist[c], 1u);
+  __shared__ TableShared T;
+  const int tid = threadIdx.x;
+  const uint64_t chunk = blockIdx.x;
+  for (int i = tid; i < 256; i += blockDim.x)
+    T.hist[i] = chunk_hist[chunk * 256 + i];
+  __syncthreads();
+  // rank the used symbols by (count, symbol) in parallel
+  for (int i = tid; i < 256; i += blockDim.x) {
+    const uint32_t fi = T.hist[i];
+    if (fi) {
+      int rank = 0;
+      for (int j = 0; j < 256; ++j) {
+        const uint32_t fj = T.hist[j];
+        rank += fj && (fj < fi || (fj == fi && j < i));
+      }
+      T.sorted[rank] = uint16_t(i);
     }
   }
-  for (uint32_t t = h + 4 * nw + lane; t < n; t += 32) {
-    const uint8_t c = in[src + t];
-    lits[dst + t] = c;
-    atomicAdd(&hist[c], 1u);
+  __syncthreads();
+  if (tid == 0) {
+    uint32_t n = 0, total = 0;
+    for (int i = 0; i < 256; ++i) {
+      n += T.hist[i] > 0;
+      total += T.hist[i];
+    }
+    T.nsym = n;
+    T.ok = 0;
+    if (total >= 256 && huff_lengths(T.hist, T.sorted, int(n), T.huff, T.hx)) {
+      huff_codes(T.huff, T.hx.rank_start, T.hx.count_w);
+      T.ok = huff_describe(T.huff, T.hx, T.tw) ? 1 : 0;
+    }
+  }
+  __syncthreads();
+  ChunkTable& ct = tables[chunk];
+  for (int c = tid; c < 256; c += blockDim.x)
+    ct.cl[c] = T.ok ? uint32_t(T.huff.code[c]) | (uint32_t(T.huff.len[c]) << 16) : 0;
+  const int dl = T.ok ? T.huff.desc_len : 0;
+  for (int i = tid; i < dl; i += blockDim.x)
+    ct.desc[i] = T.huff.desc[i];
+  if (tid == 0) {
+    ct.desc_len = uint32_t(dl);
+    ct.ok = T.ok;
   }
 }
 
@@ -655,6 +852,8 @@ zstd_block_k(CodecBatch b,
              const __grid_constant__ PredefTables pre,
              const Seq* seqs,
              const ZSeg* meta,
+             const ChunkTable* tables,
+             const uint8_t* litbuf,
              uint8_t* stage_all,
              uint32_t* block_sizes,
              uint32_t blocks_per_chunk)
@@ -674,8 +873,9 @@ zstd_block_k(CodecBatch b,
   CHUCKY_DYN_SHARED(uint8_t, lits); // this block's literals
   uint8_t* stage = stage_all + blk * kStageBytes;
 
-  for (int i = tid; i < 256 * int(kSegsPerBlock); i += blockDim.x)
-    (&S.whist[0][0])[i] = 0;
+  const ChunkTable& ct = tables[chunk];
+  for (int c = tid; c < 256; c += blockDim.x)
+    S.cl[c] = ct.cl[c];
   // the three predefined sequence tables (built once on the host)
   {
     const uint32_t* src = reinterpret_cast<const uint32_t*>(&pre);
@@ -683,12 +883,21 @@ zstd_block_k(CodecBatch b,
     for (int i = tid; i < int(sizeof(PredefTables) / 4); i += blockDim.x)
       dst[i] = src[i];
   }
+  for (int i = tid; i < 53; i += blockDim.x) {
+    S.ml_base[i] = kMLBase[i];
+    S.ml_bits[i] = kMLBits[i];
+    if (i < 36) {
+      S.ll_base[i] = kLLBase[i];
+      S.ll_bits[i] = kLLBits[i];
+    }
+  }
   if (tid == 0) {
     uint32_t carry = 0, matched_before = 0, nseq = 0;
     for (uint32_t k = 0; k < nsegs; ++k) {
       const ZSeg m = meta[segbase + k];
       const uint32_t s0 = b0 + k * kSegBytes;
       S.seg_nseq[k] = m.nseq;
+      S.seg_seq0[k] = nseq;
       S.seg_carry[k] = carry;
       S.seg_litout[k] = (s0 - b0) - matched_before; // literal slot of s0
       matched_before += m.matched;
@@ -697,120 +906,44 @@ zstd_block_k(CodecBatch b,
     }
     S.nseq = nseq;
     S.nlit = bsize - matched_before;
-    S.all_same = 1;
+    // single-valued input (RLE block) and literals (RLE literals section)
+    uint32_t all_same = 1, lit_same = 1;
+    int lit_byte = -1;
+    const uint32_t in0 = (meta[segbase].flags >> 16) & 0xFF;
+    for (uint32_t k = 0; k < nsegs; ++k) {
+      const ZSeg m = meta[segbase + k];
+      const uint32_t s0 = b0 + k * kSegBytes;
+      const uint32_t nl = min(b1, s0 + kSegBytes) - s0 - m.matched;
+      all_same &= (m.flags >> 24) & ((m.flags >> 16) & 0xFF) == in0;
+      if (nl) {
+        if (lit_byte < 0)
+          lit_byte = int(m.flags & 0xFF);
+        lit_same &= (m.flags >> 8) & ((m.flags & 0xFF) == uint32_t(lit_byte));
+      }
+    }
+    S.all_same = all_same;
+    S.lit_same = lit_same;
+    S.seq_bad = 0;
   }
   __syncthreads();
 
-  // RLE block test
-  {
-    // chunks are 16-byte aligned and blocks start at multiples of 128 KiB
-    const uint8_t first = in[b0];
-    const uint32_t pat = first * 0x01010101u;
-    bool same = true;
-    const uint32_t nv = bsize / 16;
-    const uint4* v = reinterpret_cast<const uint4*>(in + b0);
-    for (uint32_t i = tid; i < nv && same; i += blockDim.x) {
-      const uint4 q = v[i];
-      same = q.x == pat && q.y == pat && q.z == pat && q.w == pat;
-    }
-    for (uint32_t i = nv * 16 + tid; i < bsize && same; i += blockDim.x)
-      same = in[b0 + i] == first;
-    if (!same)
-      S.all_same = 0;
-  }
-
-  // gather literals: warp k copies the literal bytes that lie inside its
-  // own segment (the bytes before each match and after the last one), so
-  // all warps work even when most segments have no match at all
+  // literals: a warp per segment copies the segment's compacted literals
   if (uint32_t(warp) < nsegs) {
     const uint32_t k = warp;
     const uint32_t s0 = b0 + k * kSegBytes;
-    const uint32_t s1 = min(b1, s0 + kSegBytes);
-    const Seq* sq = seqs + (segbase + k) * kMaxSeqPerSeg;
-    const uint32_t nq = S.seg_nseq[k];
-    uint32_t src = s0, dst = S.seg_litout[k];
-    uint32_t* hist = S.whist[warp];
-    for (uint32_t base = 0; base < nq; base += 32) {
-      const uint32_t i = base + lane;
-      uint32_t ll = 0, used = 0;
-      if (i < nq) {
-        const Seq q = sq[i];
-        ll = q.lit; // this segment's own literals (no carry)
-        used = ll + q.match;
-      }
-      uint32_t ex_in = used, ex_out = ll;
-      for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t a = __shfl_up_sync(0xffffffffu, ex_in, o);
-        const uint32_t c = __shfl_up_sync(0xffffffffu, ex_out, o);
-        if (lane >= o) {
-          ex_in += a;
-          ex_out += c;
-        }
-      }
-      const uint32_t tot_in = __shfl_sync(0xffffffffu, ex_in, 31);
-      const uint32_t tot_out = __shfl_sync(0xffffffffu, ex_out, 31);
-      ex_in -= used;
-      ex_out -= ll;
-      unsigned pend = __ballot_sync(0xffffffffu, ll > 0);
-      while (pend) {
-        const int j = __ffs(pend) - 1;
-        pend &= pend - 1;
-        const uint32_t n = __shfl_sync(0xffffffffu, ll, j);
-        const uint32_t si = __shfl_sync(0xffffffffu, ex_in, j);
-        const uint32_t di = __shfl_sync(0xffffffffu, ex_out, j);
-        gather_run(in, src + si, n, lits, dst + di, hist, lane);
-      }
-      src += tot_in;
-      dst += tot_out;
-    }
-    // trailing literals of the segment (all of it when nothing matched)
-    gather_run(in, src, s1 - src, lits, dst, hist, lane);
+    const uint32_t nl = min(b1, s0 + kSegBytes) - s0 - meta[segbase + k].matched;
+    copy_bytes(lits + S.seg_litout[k], litbuf + (segbase + k) * kSegBytes, nl, lane, 32);
   }
   __syncthreads();
-  for (int i = tid; i < 256; i += blockDim.x) {
-    uint32_t t = 0;
-    for (uint32_t w = 0; w < kSegsPerBlock; ++w)
-      t += S.whist[w][i];
-    S.hist[i] = t;
-  }
-  __syncthreads();
-  // rank the used symbols by (count, symbol) in parallel for the Huffman
-  // build (one comparison pass per symbol instead of a serial sort)
-  for (int i = tid; i < 256; i += blockDim.x) {
-    const uint32_t fi = S.hist[i];
-    if (fi) {
-      int rank = 0;
-      for (int j = 0; j < 256; ++j) {
-        const uint32_t fj = S.hist[j];
-        rank += fj && (fj < fi || (fj == fi && j < i));
-      }
-      S.sorted[rank] = uint16_t(i);
-    }
-  }
-  if (tid == 0) {
-    uint32_t n = 0;
-    for (int i = 0; i < 256; ++i)
-      n += S.hist[i] > 0;
-    S.nsym = n;
-  }
-  __syncthreads();
-
   const uint32_t nlit = S.nlit, nseq = S.nseq;
   if (tid == 0) {
     // literals section mode (the exact Huffman size decides below)
     S.lit_mode = 0;
-    if (nlit > 0 && S.nsym == 1)
+    if (nlit > 0 && S.lit_same)
       S.lit_mode = 1;
-    else if (nlit >= 256 &&
-             huff_lengths(S.hist, S.sorted, S.nsym, S.huff, S.hx)) {
-      huff_codes(S.huff, S.hx.rank_start, S.hx.count_w);
-      if (huff_describe(S.huff, S.hx, S.tw))
-        S.lit_mode = 2;
-    }
+    else if (nlit >= 256 && ct.ok)
+      S.lit_mode = 2;
   }
-  __syncthreads();
-  for (int c = tid; c < 256; c += blockDim.x)
-    S.huff.cl[c] = uint32_t(S.huff.code[c]) | (uint32_t(S.huff.len[c]) << 16);
   __syncthreads();
 
   // ---- Huffman streams: bit lengths per stream (64 threads per stream)
@@ -824,19 +957,29 @@ zstd_block_k(CodecBatch b,
     const uint32_t q0 = uint32_t(uint64_t(m) * t / kStreamThreads);
     const uint32_t q1 = uint32_t(uint64_t(m) * (t + 1) / kStreamThreads);
     uint32_t bits = 0;
-    const uint32_t* cl = S.huff.cl;
+    const uint32_t* cl = S.cl;
     for_each_desc(lits, a1 - q1, a1 - q0,
                   [&](uint8_t c) { bits += cl[c] >> 16; });
-    // exclusive scan over the stream's warp
+    // exclusive scan over the stream's threads (whole warps)
     uint32_t before = bits;
     for (int o = 1; o < 32; o <<= 1) {
       const uint32_t y = __shfl_up_sync(0xffffffffu, before, o);
-      if (t >= o)
+      if (lane >= o)
         before += y;
     }
-    if (t == kStreamThreads - 1)
-      S.stream_bits[st] = before;
+    if (lane == 31)
+      S.warp_bits[warp] = before;
     before -= bits;
+    __syncthreads();
+    constexpr int kStreamWarps = kStreamThreads / 32;
+    for (int w = st * kStreamWarps; w < warp; ++w)
+      before += S.warp_bits[w];
+    if (tid < 4) {
+      uint32_t sb = 0;
+      for (int w = 0; w < kStreamWarps; ++w)
+        sb += S.warp_bits[tid * kStreamWarps + w];
+      S.stream_bits[tid] = sb;
+    }
     __syncthreads();
     if (tid == 0) {
       // literals section layout
@@ -845,12 +988,13 @@ zstd_block_k(CodecBatch b,
         ssz[s] = S.stream_bits[s] / 8 + 1; // end mark + padding
         tot += ssz[s];
       }
-      const uint32_t csize = S.huff.desc_len + 6 + tot;
+      const uint32_t dlen = ct.desc_len;
+      const uint32_t csize = dlen + 6 + tot;
       const uint32_t big = max(nlit, csize);
       const uint32_t hdr = big < 1024 ? 3 : (big < 16384 ? 4 : 5);
       S.lit_hdr = hdr;
       S.lit_size = hdr + csize;
-      uint32_t pos = 3 + hdr + S.huff.desc_len + 6;
+      uint32_t pos = 3 + hdr + dlen + 6;
       for (int s = 0; s < 4; ++s) {
         S.stream_pos[s] = pos;
         pos += ssz[s];
@@ -865,9 +1009,9 @@ zstd_block_k(CodecBatch b,
                            (uint64_t(csize) << (4 + nbits));
         put_le(o, h, hdr);
         o += hdr;
-        for (int i = 0; i < S.huff.desc_len; ++i)
-          o[i] = S.huff.desc[i];
-        o += S.huff.desc_len;
+        for (uint32_t i = 0; i < dlen; ++i)
+          o[i] = ct.desc[i];
+        o += dlen;
         put_le(o, ssz[0], 2);
         put_le(o + 2, ssz[1], 2);
         put_le(o + 4, ssz[2], 2);
@@ -896,7 +1040,7 @@ zstd_block_k(CodecBatch b,
       const bool first_shared = fill != 0;
       bool first = true;
       uint64_t acc = 0;
-      const uint32_t* cl = S.huff.cl;
+      const uint32_t* cl = S.cl;
       for_each_desc(lits, a1 - q1, a1 - q0, [&](uint8_t c) {
         const uint32_t e = cl[c];
         acc |= uint64_t(e & 0xFFFF) << fill;
@@ -959,68 +1103,111 @@ zstd_block_k(CodecBatch b,
   }
   __syncthreads();
 
-  // ---- sequences section (thread 0)
-  if (tid == 0) {
-    uint8_t* o = stage + 3 + S.lit_size;
-    // every sequence takes at most 9 bytes of the bitstream
-    const bool fits = 3 + uint64_t(S.lit_size) + 8 + 9 * uint64_t(nseq) <
-                      kStageBytes;
-    if (!fits)
-      o = stage; // contents unused: the block is written raw below
-    bool bad = false;
-    if (nseq < 128)
-      *o++ = uint8_t(nseq);
-    else if (nseq < 0x7F00) {
-      *o++ = uint8_t((nseq >> 8) + 128);
-      *o++ = uint8_t(nseq);
-    } else {
-      *o++ = 255;
-      put_le(o, nseq - 0x7F00, 2);
-      o += 2;
+  // ---- sequences section.  The three FSE state chains (LL, ML, OF) are
+  // serial by nature: lanes 0-2 of warp 0 walk them side by side and record
+  // the state every sequence starts from.  Everything else -- codes, bit
+  // counts, the block-wide scan of bit positions and the bit packing -- runs
+  // on all threads.  The literal buffer is free again (the literals are in
+  // staging) and holds the per-sequence codes, then the states.
+  uint8_t* scode = lits; // [3][nseq]: LL, ML, OF codes -> states (in place)
+  for (uint32_t j = tid; j < nseq; j += blockDim.x) {
+    uint32_t ll, ml, off;
+    seq_at(S, seqs, segbase, nsegs, j, ll, ml, off);
+    const int oc = highbit(off);
+    if (oc > 28 || ml < 3 || off <= 3)
+      S.seq_bad = 1;
+    scode[j] = uint8_t(ll_code_s(ll, S.ll_base));
+    scode[nseq + j] = uint8_t(ml_code_s(ml, S.ml_base));
+    scode[2 * nseq + j] = uint8_t(oc);
+  }
+  __syncthreads();
+  if (warp == 0 && lane < 3 && nseq) {
+    const FseEnc& t = lane == 0 ? S.pre.ll : (lane == 1 ? S.pre.ml : S.pre.of);
+    uint8_t* a = scode + lane * nseq;
+    const uint32_t size = 1u << t.al;
+    uint32_t v = t.states[t.first[a[nseq - 1]]] + size;
+    for (int j = int(nseq) - 2; j >= 0; --j) {
+      const int sym = a[j];
+      a[j] = uint8_t(v - size);
+      const int c = t.count[sym];
+      int nb = t.al - highbit(uint32_t(c));
+      if ((v >> nb) < uint32_t(c))
+        --nb;
+      v = t.states[t.first[sym] + ((v >> nb) - c)] + size;
     }
-    if (nseq && fits) {
-      *o++ = 0; // predefined LL, OF and ML tables
-      const FseEnc& tll = S.pre.ll;
-      const FseEnc& tml = S.pre.ml;
-      const FseEnc& tof = S.pre.of;
-      BitOut bo;
-      bo.init(o);
-      // walk the sequences backwards across segments
-      uint32_t vll = 0, vml = 0, vof = 0;
-      bool first = true;
-      for (int k = int(nsegs) - 1; k >= 0 && !bad; --k) {
-        const Seq* sq = seqs + (segbase + k) * kMaxSeqPerSeg;
-        for (int i = int(S.seg_nseq[k]) - 1; i >= 0; --i) {
-          const Seq q = sq[i];
-          const uint32_t ll = q.lit + (i == 0 ? S.seg_carry[k] : 0);
-          const uint32_t off = q.offset + 3;
-          const int lc = ll_code(ll), mc = ml_code(q.match);
-          const int oc = highbit(off);
-          if (oc > 28 || q.match < 3 || q.offset == 0) { // cannot happen
-            bad = true;
-            break;
-          }
-          if (first) {
-            vll = fse_init(tll, lc);
-            vml = fse_init(tml, mc);
-            vof = fse_init(tof, oc);
-            first = false;
-          } else {
-            fse_encode(tof, vof, oc, bo);
-            fse_encode(tml, vml, mc, bo);
-            fse_encode(tll, vll, lc, bo);
-          }
-          bo.put(ll - kLLBase[lc], kLLBits[lc]);
-          bo.put(q.match - kMLBase[mc], kMLBits[mc]);
-          bo.put(off - (1u << oc), oc);
-        }
+    S.final_state[lane] = v - size;
+  }
+  __syncthreads();
+  // sequence p of the stream is block sequence nseq - 1 - p (written
+  // backwards); thread tid packs the stream sequences [p0, p1)
+  const uint32_t p0 = uint32_t(uint64_t(nseq) * tid / kBlockThreads);
+  const uint32_t p1 = uint32_t(uint64_t(nseq) * (tid + 1) / kBlockThreads);
+  uint32_t my_bits = 0;
+  for (uint32_t p = p0; p < p1; ++p)
+    my_bits += seq_emit(S, seqs, segbase, nsegs, nseq, scode, nseq - 1 - p,
+                        [](uint32_t, int) {});
+  uint32_t before = my_bits;
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, before, o);
+    if (lane >= o)
+      before += y;
+  }
+  if (lane == 31)
+    S.warp_bits[warp] = before;
+  before -= my_bits;
+  __syncthreads();
+  uint32_t total_bits = 0;
+  for (int w = 0; w < kBlockThreads / 32; ++w) {
+    if (w < warp)
+      before += S.warp_bits[w];
+    total_bits += S.warp_bits[w];
+  }
+  // header: sequence count, then the modes byte (predefined tables)
+  const uint32_t seq_at0 = 3 + S.lit_size;
+  const uint32_t nhdr = nseq == 0 ? 1 : (nseq < 128 ? 2 : (nseq < 0x7F00 ? 3 : 4));
+  const uint32_t bs0 = seq_at0 + nhdr; // first byte of the bitstream
+  // 17 bits of final states and the end mark
+  const uint32_t nbytes = nseq ? (total_bits + 17 + 1 + 7) / 8 : 0;
+  const bool fits = bs0 + nbytes + 4 <= kStageBytes && !S.seq_bad;
+  if (fits) {
+    if (tid == 0) {
+      uint8_t* o = stage + seq_at0;
+      if (nseq < 128)
+        *o++ = uint8_t(nseq);
+      else if (nseq < 0x7F00) {
+        *o++ = uint8_t((nseq >> 8) + 128);
+        *o++ = uint8_t(nseq);
+      } else {
+        *o++ = 255;
+        put_le(o, nseq - 0x7F00, 2);
+        o += 2;
       }
-      bo.put(vml - 64, 6);
-      bo.put(vof - 32, 5);
-      bo.put(vll - 64, 6);
-      o = bo.close();
+      if (nseq)
+        *o = 0; // predefined LL, OF and ML tables
     }
-    uint32_t csize = (fits && !bad) ? uint32_t(o - (stage + 3)) : bsize;
+    for (uint32_t i = bs0 + tid; i < bs0 + nbytes + 4; i += blockDim.x)
+      stage[i] = 0;
+  }
+  __syncthreads();
+  if (fits && nseq) {
+    BitPack bp;
+    bp.init(stage + bs0, before);
+    for (uint32_t p = p0; p < p1; ++p)
+      seq_emit(S, seqs, segbase, nsegs, nseq, scode, nseq - 1 - p,
+               [&](uint32_t v, int n) { bp.put(v, n); });
+    if (p1 == nseq && p1 > p0) { // the stream's last sequence: states, end mark
+      bp.put(S.final_state[1], 6);
+      bp.put(S.final_state[2], 5);
+      bp.put(S.final_state[0], 6);
+      bp.put(1, 1);
+    }
+    bp.flush();
+  }
+  if (tid == 0)
+    S.seq_csize = fits ? bs0 + nbytes - 3 : 0xFFFFFFFFu;
+  __syncthreads();
+  if (tid == 0) {
+    const uint32_t csize = min(S.seq_csize, bsize);
     const bool last = b1 == b.chunk_bytes;
     uint32_t total;
     if (S.all_same) { // RLE block: one byte
@@ -1096,8 +1283,9 @@ size_t zstd_scratch_bytes(uint64_t n_chunks, uint32_t chunk_bytes)
   const uint64_t segs = n_chunks * ((chunk_bytes + kSegBytes - 1) / kSegBytes);
   const uint64_t blocks =
     n_chunks * ((chunk_bytes + kBlockBytes - 1) / kBlockBytes);
-  return segs * (kMaxSeqPerSeg * sizeof(Seq) + sizeof(ZSeg)) +
-         blocks * (kStageBytes + sizeof(uint32_t)) + 1024;
+  return segs * (kMaxSeqPerSeg * sizeof(Seq) + sizeof(ZSeg) + kSegBytes) +
+         blocks * (kStageBytes + sizeof(uint32_t)) +
+         n_chunks * (256 * sizeof(uint32_t) + sizeof(ChunkTable)) + 2048;
 }
 
 cudaError_t launch_zstd(CodecBatch b, void* scratch, cudaStream_t st)
@@ -1119,9 +1307,23 @@ cudaError_t launch_zstd(CodecBatch b, void* scratch, cudaStream_t st)
   uint8_t* stage = p;
   p += blocks * kStageBytes;
   uint32_t* bsizes = reinterpret_cast<uint32_t*>(p);
+  p += blocks * sizeof(uint32_t);
+  p = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(p) + 255) & ~uintptr_t(255));
+  uint32_t* hist = reinterpret_cast<uint32_t*>(p);
+  p += b.n_chunks * 256 * sizeof(uint32_t);
+  ChunkTable* tables = reinterpret_cast<ChunkTable*>(p);
+  p += b.n_chunks * sizeof(ChunkTable);
+  p = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(p) + 255) & ~uintptr_t(255));
+  uint8_t* litbuf = p; // segs * kSegBytes, read up to 20 bytes past a slot
+  const uint32_t rpc = (b.chunk_bytes + kRegionBytes - 1) / kRegionBytes;
   cudaError_t e;
-  note_launches(3);
-  CHUCKY_LAUNCH(zstd_find_k, unsigned((segs + kFindWarps - 1) / kFindWarps), 32 * kFindWarps, 0, st, b, seqs, meta);
+  if ((e = cudaMemsetAsync(hist, 0, b.n_chunks * 256 * sizeof(uint32_t), st)) !=
+      cudaSuccess)
+    return e;
+  note_launches(4);
+  CHUCKY_LAUNCH(zstd_find_k, unsigned(b.n_chunks * rpc), 32 * kSegsPerRegion,
+                kRegionStageWords * sizeof(uint32_t), st, b, seqs, meta, hist, litbuf,
+                rpc);
   if ((e = cudaGetLastError()) != cudaSuccess)
     return e;
   static const PredefTables pre = [] {
@@ -1132,8 +1334,11 @@ cudaError_t launch_zstd(CodecBatch b, void* scratch, cudaStream_t st)
     fse_build(t.of, kOFNormH, 29, 5, spread, fill);
     return t;
   }();
-  CHUCKY_LAUNCH(zstd_block_k, unsigned(blocks), kBlockThreads, kBlockBytes + 16, st, b, pre, seqs, meta,
-                                                           stage, bsizes, bpc);
+  CHUCKY_LAUNCH(zstd_table_k, unsigned(b.n_chunks), kBlockThreads, 0, st, hist, tables);
+  if ((e = cudaGetLastError()) != cudaSuccess)
+    return e;
+  CHUCKY_LAUNCH(zstd_block_k, unsigned(blocks), kBlockThreads, kBlockBytes + 16, st, b,
+                pre, seqs, meta, tables, litbuf, stage, bsizes, bpc);
   if ((e = cudaGetLastError()) != cudaSuccess)
     return e;
   CHUCKY_LAUNCH(zstd_frame_k, unsigned(b.n_chunks), 256, 0, st, b, stage, bsizes, bpc);

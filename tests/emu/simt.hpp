@@ -47,6 +47,11 @@ struct uint4
   unsigned x, y, z, w;
 };
 
+inline uint4 make_uint4(unsigned x, unsigned y, unsigned z, unsigned w)
+{
+  return uint4{ x, y, z, w };
+}
+
 struct dim3
 {
   unsigned x = 1, y = 1, z = 1;
@@ -134,6 +139,10 @@ inline unsigned __ballot_sync(unsigned, int pred)
   simt::warp_sync();
   return m;
 }
+inline int __all_sync(unsigned mask, int pred)
+{
+  return __ballot_sync(mask, pred) == 0xffffffffu;
+}
 inline unsigned __match_any_sync(unsigned, unsigned v)
 {
   const unsigned me = threadIdx.x, base = me & ~31u;
@@ -182,6 +191,12 @@ inline unsigned atomicOr(unsigned* p, unsigned v)
     simt::fail("misaligned 32-bit atomicOr");
   return std::atomic_ref<unsigned>(*p).fetch_or(v);
 }
+inline unsigned atomicAnd(unsigned* p, unsigned v)
+{
+  if (reinterpret_cast<uintptr_t>(p) & 3)
+    simt::fail("misaligned 32-bit atomicAnd");
+  return std::atomic_ref<unsigned>(*p).fetch_and(v);
+}
 using std::max;
 using std::min;
 
@@ -197,6 +212,23 @@ void launch(unsigned grid, unsigned block, const std::function<void()>& body);
   simt::launch(unsigned(grid), unsigned(block), [&] { kernel(__VA_ARGS__); })
 
 inline cudaError_t cudaGetLastError()
+{
+  return cudaSuccess;
+}
+
+inline cudaError_t cudaMemsetAsync(void* p, int v, size_t n, cudaStream_t = nullptr)
+{
+  std::memset(p, v, n);
+  return cudaSuccess;
+}
+
+enum cudaFuncAttribute
+{
+  cudaFuncAttributeMaxDynamicSharedMemorySize = 8
+};
+
+template<typename F>
+inline cudaError_t cudaFuncSetAttribute(F, cudaFuncAttribute, int)
 {
   return cudaSuccess;
 }
