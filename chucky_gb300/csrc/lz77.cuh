@@ -10,7 +10,9 @@
 // matches may reach back to the start of the region, as a single parse of
 // the region would; the segments are parsed side by side.
 //
-// The segment is scanned in windows of 32 positions, one per lane.  Every
+// The segment is scanned in windows of 32 positions, one per lane (with a
+// stride that grows by one for every 2^kSearchStrength literals since the
+// last match, as fast LZ77 parsers skip through incompressible data).  Every
 // lane hashes the 4 bytes at its position, probes the table, verifies the
 // candidate (or, for runs and periods of 1, 2 or 4 bytes, the lane 1, 2 or
 // 4 positions back in the same window) and measures the match on its own,
@@ -43,6 +45,17 @@ constexpr uint32_t kMaxSeqPerSeg = kSegBytes / 4 + 1;
 constexpr uint32_t kRegionStageWords = kRegionBytes / 4 + 4;
 // bytes a lane measures of its own match before the warp takes over
 constexpr uint32_t kLaneExtend = 64;
+#ifndef CHUCKY_SEARCH_STRENGTH
+#define CHUCKY_SEARCH_STRENGTH 8
+#endif
+#ifndef CHUCKY_HISTORY_SEGS
+#define CHUCKY_HISTORY_SEGS 3
+#endif
+// positions probed per lane step grow by one for every 2^kSearchStrength
+// literals since the last match (sparse probing of incompressible runs)
+constexpr int kSearchStrength = CHUCKY_SEARCH_STRENGTH;
+// segments of the region before a warp's own that enter its table
+constexpr uint32_t kHistorySegs = CHUCKY_HISTORY_SEGS;
 static_assert((2u << kHashLog) >= kSegBytes / 8,
               "a warp's table holds its literal bitmap");
 
@@ -124,7 +137,9 @@ __device__ inline SegInfo lz77_parse_segment(const uint32_t* words,
   const uint32_t lim = start_limit > s0 ? start_limit - r0 : first;
   const uint32_t end = match_end - r0;
   // history: the region's positions before this segment
-  for (uint32_t w0 = 0; w0 < first; w0 += 32) {
+  const uint32_t hist0 =
+    first > kHistorySegs * kSegBytes ? first - kHistorySegs * kSegBytes : 0;
+  for (uint32_t w0 = hist0; w0 < first; w0 += 32) {
     const uint32_t q = w0 + lane;
     const uint32_t h = hash4(word_at(words, q));
     __syncwarp();
@@ -133,7 +148,8 @@ __device__ inline SegInfo lz77_parse_segment(const uint32_t* words,
   __syncwarp();
   uint32_t w0 = first, p = first, lit_start = first, nseq = 0;
   while (w0 < lim) {
-    const uint32_t q = w0 + lane;
+    const uint32_t step = 1 + ((w0 > lit_start ? w0 - lit_start : 0) >> kSearchStrength);
+    const uint32_t q = w0 + lane * step;
     const bool valid = q < lim && q + 4 <= end;
     uint32_t v = 0, h = 0, cand = 0;
     bool ok = false;
@@ -156,13 +172,13 @@ __device__ inline SegInfo lz77_parse_segment(const uint32_t* words,
       const uint32_t v4 = __shfl_up_sync(0xffffffffu, v, 4);
       if (valid && !ok) {
         if (lane >= 1 && v1 == v) {
-          cand = q - 1;
+          cand = q - step;
           ok = true;
         } else if (lane >= 2 && v2 == v) {
-          cand = q - 2;
+          cand = q - 2 * step;
           ok = true;
         } else if (lane >= 4 && v4 == v) {
-          cand = q - 4;
+          cand = q - 4 * step;
           ok = true;
         }
       }
@@ -192,14 +208,15 @@ __device__ inline SegInfo lz77_parse_segment(const uint32_t* words,
     unsigned hits = __ballot_sync(0xffffffffu, ok && len >= min_match);
     // greedy parse through this window
     for (;;) {
-      const uint32_t from = p > w0 ? p - w0 : 0;
+      // first lane at or after the parse point
+      const uint32_t from = p > w0 ? (p - w0 + step - 1) / step : 0;
       if (from >= 32)
         break;
       const unsigned m = hits & (0xffffffffu << from);
       if (!m)
         break;
       const int k = __ffs(int(m)) - 1;
-      const uint32_t mpos = w0 + k;
+      const uint32_t mpos = w0 + k * step;
       const uint32_t src = __shfl_sync(0xffffffffu, cand, k);
       uint32_t mlen = __shfl_sync(0xffffffffu, len, k);
       if (mlen >= kLaneExtend) { // long match: the warp extends it
@@ -222,7 +239,7 @@ __device__ inline SegInfo lz77_parse_segment(const uint32_t* words,
       lit_start = p;
     }
     // next window; skip windows that lie inside a long match
-    w0 = p >= w0 + 64 ? p : w0 + 32;
+    w0 = p >= w0 + 64 * step ? p : w0 + 32 * step;
   }
   __syncwarp();
   return SegInfo{ nseq, (s1 - r0) - lit_start };
@@ -233,18 +250,18 @@ __device__ inline SegInfo lz77_parse_segment(const uint32_t* words,
 // staged region; returns their count.  Call after every warp of the CTA
 // has finished parsing (the region is no longer read as history).
 // `bitmap` is kSegBytes / 8 bytes of the warp's (free again) hash table.
-// `hist` (256 counts, zeroed) receives the literal bytes when not null.
 __device__ inline uint32_t lz77_compact_literals(uint32_t* words,
                                                  uint32_t r0,
                                                  uint32_t s0,
                                                  uint32_t s1,
                                                  const Seq* sq,
                                                  uint32_t nseq,
-                                                 uint32_t* bitmap,
-                                                 uint32_t* hist)
+                                                 uint32_t* bitmap)
 {
   const unsigned lane = threadIdx.x & 31;
   const uint32_t n = s1 - s0;
+  if (nseq == 0) // every byte is a literal, already in place
+    return n;
   const uint32_t nwords = (n + 31) >> 5;
   // bit i of word j: position 32 j + i is a literal
   for (uint32_t j = lane; j < nwords; j += 32) {
@@ -287,8 +304,11 @@ __device__ inline uint32_t lz77_compact_literals(uint32_t* words,
   __syncwarp();
   // compact 1 KiB at a time: every lane reads its 32 bytes into registers,
   // then writes their literal bytes at the final place (never after the
-  // source, so later bytes are still intact)
+  // source, so later bytes are still intact).  Lanes start at different
+  // bytes of their word (the place of each byte follows from the bitmap)
+  // so that their stores fall in different banks.
   uint8_t* bytes = reinterpret_cast<uint8_t*>(words) + (s0 - r0);
+  const int rot = int(lane & 7) * 4;
   uint32_t out = 0;
   for (uint32_t c = 0; c < nwords; c += 32) {
     const uint32_t j = c + lane;
@@ -310,16 +330,14 @@ __device__ inline uint32_t lz77_compact_literals(uint32_t* words,
     const uint32_t tot = __shfl_sync(0xffffffffu, ex, 31);
     ex -= cnt;
     __syncwarp();
-    uint32_t d = out + ex;
-    while (m) {
-      const int i = __ffs(int(m)) - 1;
-      m &= m - 1;
+    const uint32_t d = out + ex;
+    uint32_t mr = __funnelshift_r(m, m, rot); // m rotated right by rot
+    while (mr) {
+      const int i = (__ffs(int(mr)) - 1 + rot) & 31;
+      mr &= mr - 1;
       const uint32_t wd = i < 16 ? (i < 8 ? (i < 4 ? lo4.x : lo4.y) : (i < 12 ? lo4.z : lo4.w))
                                  : (i < 24 ? (i < 20 ? hi4.x : hi4.y) : (i < 28 ? hi4.z : hi4.w));
-      const uint8_t c8 = uint8_t(wd >> ((i & 3) * 8));
-      bytes[d++] = c8;
-      if (hist)
-        atomicAdd(hist + c8, 1u);
+      bytes[d + __popc(m & ((1u << i) - 1))] = uint8_t(wd >> ((i & 3) * 8));
     }
     out += tot;
     __syncwarp();

@@ -252,22 +252,33 @@ zstd_find_k(CodecBatch b,
   const uint8_t* sb = reinterpret_cast<const uint8_t*>(words) + (s0 - r0);
   const uint32_t n = s1 - s0;
   const uint8_t in0 = sb[0];
+  const uint32_t pat = in0 * 0x01010101u;
+  const uint32_t* sw = words + (s0 - r0) / 4;
   bool same = true;
-  for (uint32_t i = lane; i < n; i += 32)
+  for (uint32_t i = lane; i < n / 4; i += 32)
+    same &= sw[i] == pat;
+  for (uint32_t i = n / 4 * 4 + lane; i < n; i += 32)
     same &= sb[i] == in0;
   const bool in_same = __all_sync(0xffffffffu, same);
   // literals: compacted in place, counted, copied out
   uint32_t* bitmap = reinterpret_cast<uint32_t*>(tables[w]);
   uint32_t* hist = bitmap + (kSegBytes / 32 + 31) / 32 * 32; // after the bitmap
+  static_assert((kSegBytes / 32 + 31) / 32 * 32 + 256 <= (1u << kHashLog) / 2,
+                "bitmap and histogram fit in a warp's table");
   for (int i = lane; i < 256; i += 32)
     hist[i] = 0;
   __syncwarp();
-  const uint32_t nlit =
-    lz77_compact_literals(words, r0, s0, s1, out, info.nseq, bitmap, hist);
+  const uint32_t nlit = lz77_compact_literals(words, r0, s0, s1, out, info.nseq, bitmap);
+  __syncwarp();
+  // count the literals (consecutive lanes, consecutive bytes: few lanes
+  // share a symbol within one step) and test whether they are one value
   const uint8_t lit0 = nlit ? sb[0] : 0;
   same = true;
-  for (uint32_t i = lane; i < nlit; i += 32)
-    same &= sb[i] == lit0;
+  for (uint32_t i = lane; i < nlit; i += 32) {
+    const uint8_t c = sb[i];
+    atomicAdd(hist + c, 1u);
+    same &= c == lit0;
+  }
   const bool lit_same = __all_sync(0xffffffffu, same);
   const uint4* src = reinterpret_cast<const uint4*>(sb);
   uint4* dst = reinterpret_cast<uint4*>(litbuf + seg * kSegBytes);
@@ -314,107 +325,6 @@ struct Huff
   int desc_len;
   uint64_t bits;       // sum of code lengths over the literals
 };
-
-// Code lengths limited to kHufMaxBits, complete prefix code.  Two-queue
-// Huffman on the sorted leaves, then clamp + Kraft repair.
-__device__ bool huff_lengths(const uint32_t* freq,
-                             const uint16_t* sorted,
-                             int n,
-                             Huff& h,
-                             HuffScratch& x)
-{
-  // `sorted`: the n symbols with freq > 0, ascending by (freq, symbol)
-  uint16_t* sym = x.sym;
-  uint32_t* f = x.f;
-  int16_t* parent = x.parent;
-  if (n < 2)
-    return false;
-  for (int i = 0; i < n; ++i)
-    sym[i] = sorted[i];
-  for (int i = 0; i < n; ++i)
-    f[i] = freq[sym[i]];
-  int leaf = 0, inode = n, next = n;
-  for (int k = 0; k < n - 1; ++k) {
-    int pick[2];
-    for (int t = 0; t < 2; ++t) {
-      if (leaf < n && (inode >= next || f[leaf] <= f[inode]))
-        pick[t] = leaf++;
-      else
-        pick[t] = inode++;
-    }
-    f[next] = f[pick[0]] + f[pick[1]];
-    parent[pick[0]] = parent[pick[1]] = int16_t(next);
-    ++next;
-  }
-  uint8_t* depth = x.depth;
-  depth[next - 1] = 0;
-  for (int i = next - 2; i >= 0; --i)
-    depth[i] = uint8_t(depth[parent[i]] + 1);
-  for (int s = 0; s < 256; ++s)
-    h.len[s] = 0;
-  int maxlen = 0;
-  for (int i = 0; i < n; ++i) {
-    int L = depth[i];
-    if (L > int(kHufMaxBits))
-      L = kHufMaxBits;
-    h.len[sym[i]] = uint8_t(L);
-    maxlen = L > maxlen ? L : maxlen;
-  }
-  // Kraft repair at maxlen: sum of 2^(maxlen-len) must equal 2^maxlen
-  const uint32_t full = 1u << maxlen;
-  uint32_t kraft = 0;
-  for (int i = 0; i < n; ++i)
-    kraft += 1u << (maxlen - h.len[sym[i]]);
-  // over-full: lengthen the least frequent codes shorter than maxlen
-  while (kraft > full) {
-    for (int i = 0; i < n && kraft > full; ++i) {
-      const int s = sym[i];
-      if (h.len[s] < maxlen) {
-        kraft -= 1u << (maxlen - h.len[s] - 1);
-        h.len[s]++;
-      }
-    }
-  }
-  // under-full: shorten the most frequent codes that still fit
-  for (int i = n - 1; i >= 0 && kraft < full; --i) {
-    const int s = sym[i];
-    while (h.len[s] > 1 && kraft + (1u << (maxlen - h.len[s])) <= full) {
-      kraft += 1u << (maxlen - h.len[s]);
-      h.len[s]--;
-    }
-  }
-  if (kraft != full)
-    return false;
-  h.max_bits = 0;
-  for (int s = 0; s < 256; ++s)
-    h.max_bits = h.len[s] > h.max_bits ? h.len[s] : h.max_bits;
-  return true;
-}
-
-// Canonical codes in zstd's order: by weight ascending (longest code
-// first), then by symbol (RFC 8878 4.2.1.3).
-__device__ void huff_codes(Huff& h, uint32_t* rank_start, uint32_t* count_w)
-{
-  const int mb = h.max_bits;
-  for (int i = 0; i < 16; ++i)
-    rank_start[i] = count_w[i] = 0;
-  for (int s = 0; s < 256; ++s)
-    if (h.len[s])
-      count_w[mb + 1 - h.len[s]]++;
-  uint32_t acc = 0;
-  for (int w = 1; w <= mb; ++w) {
-    rank_start[w] = acc;
-    acc += count_w[w] << (w - 1);
-  }
-  h.last = 0;
-  for (int s = 0; s < 256; ++s)
-    if (h.len[s]) {
-      const int w = mb + 1 - h.len[s];
-      h.code[s] = uint16_t(rank_start[w] >> (w - 1));
-      rank_start[w] += 1u << (w - 1);
-      h.last = s;
-    }
-}
 
 // Normalize a histogram of weights to 2^al, every present symbol >= 1 and
 // no symbol above half the table (so every state reads >= 1 bit and the
@@ -527,12 +437,11 @@ __device__ int write_ncount(uint8_t* out, const int16_t* norm, int nsym, int al)
 }
 
 // Tree description: direct 4-bit weights when <= 128 weights, else FSE.
+// x.w holds the weights of symbols 0 .. h.last - 1.
 __device__ bool huff_describe(Huff& h, HuffScratch& x, FseEnc& t)
 {
-  const int mb = h.max_bits, nw = h.last; // explicit weights: symbols < last
-  uint8_t* w = x.w;
-  for (int s = 0; s < nw; ++s)
-    w[s] = h.len[s] ? uint8_t(mb + 1 - h.len[s]) : 0;
+  const int nw = h.last; // explicit weights: symbols < last (in x.w)
+  const uint8_t* w = x.w;
   if (nw <= 128) {
     h.desc[0] = uint8_t(127 + nw);
     for (int i = 0; i < (nw + 1) / 2; ++i) {
@@ -603,7 +512,7 @@ struct TableShared
 {
   uint32_t hist[256];
   uint16_t sorted[256]; // used symbols by (count, symbol)
-  uint32_t nsym;
+  uint32_t nsym, total;
   uint32_t ok;
   FseEnc tw;            // Huffman weights table
   HuffScratch hx;
@@ -625,6 +534,7 @@ struct BlockShared
   uint32_t lit_hdr;       // literals section header bytes
   uint32_t lit_size;      // literals section bytes (header included)
   uint32_t lit_same;      // every literal equals the first
+  uint32_t lit_missing;   // a literal has no code in the chunk's table
   uint32_t all_same;
   // sequences section
   uint32_t ll_base[36], ml_base[53];
@@ -774,26 +684,26 @@ __device__ __forceinline__ uint32_t seq_emit(const BlockShared& S,
   return bits + lb + mb + oc;
 }
 
-// Visit lits[hi-1], lits[hi-2], ..., lits[lo] (descending), reading the
-// shared-memory literal buffer 16 bytes at a time.
-template<typename F>
-__device__ __forceinline__ void for_each_desc(const uint8_t* lits,
-                                              uint32_t lo,
-                                              uint32_t hi,
-                                              F&& f)
+// Visit lits[hi-1], lits[hi-2], ..., lits[lo] (descending): the unaligned
+// ends byte by byte through f1, every whole aligned 16-byte word of the
+// shared-memory literal buffer at once through f16 (which takes its bytes
+// 15, 14, ..., 0).
+template<typename F1, typename F16>
+__device__ __forceinline__ void visit_desc(const uint8_t* lits,
+                                           uint32_t lo,
+                                           uint32_t hi,
+                                           F1&& f1,
+                                           F16&& f16)
 {
   uint32_t a = hi;
-  while (a > lo) {
-    const uint32_t wi = (a - 1) >> 4;
-    const uint4 w = reinterpret_cast<const uint4*>(lits)[wi];
-    const uint32_t wlo = max(lo, wi << 4);
-    for (uint32_t x = a; x > wlo; --x) {
-      const uint32_t o = (x - 1) & 15;
-      const uint32_t word = o < 4 ? w.x : (o < 8 ? w.y : (o < 12 ? w.z : w.w));
-      f(uint8_t(word >> ((o & 3) * 8)));
-    }
-    a = wlo;
+  while (a > lo && (a & 15))
+    f1(lits[--a]);
+  while (a >= lo + 16) {
+    a -= 16;
+    f16(*reinterpret_cast<const uint4*>(lits + a));
   }
+  while (a > lo)
+    f1(lits[--a]);
 }
 
 // One CTA per chunk: the length-limited Huffman code of the chunk's
@@ -802,45 +712,188 @@ __device__ __forceinline__ void for_each_desc(const uint8_t* lits,
 __global__ void __launch_bounds__(kBlockThreads)
 zstd_table_k(const uint32_t* chunk_hist, ChunkTable* tables)
 {
+  static_assert(kBlockThreads >= 256, "a thread per symbol");
   __shared__ TableShared T;
-  const int tid = threadIdx.x;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const uint64_t chunk = blockIdx.x;
-  for (int i = tid; i < 256; i += blockDim.x)
-    T.hist[i] = chunk_hist[chunk * 256 + i];
+  HuffScratch& x = T.hx;
+  Huff& h = T.huff;
+  if (tid < 256) {
+    T.hist[tid] = chunk_hist[chunk * 256 + tid];
+    h.len[tid] = 0;
+  }
+  if (tid < 16)
+    x.count_w[tid] = x.whist[tid] = 0;
+  if (tid == 0)
+    T.nsym = T.total = 0;
   __syncthreads();
-  // rank the used symbols by (count, symbol) in parallel
-  for (int i = tid; i < 256; i += blockDim.x) {
-    const uint32_t fi = T.hist[i];
+  // rank the used symbols by (count, symbol); count them
+  if (tid < 256) {
+    const uint32_t fi = T.hist[tid];
     if (fi) {
       int rank = 0;
       for (int j = 0; j < 256; ++j) {
         const uint32_t fj = T.hist[j];
-        rank += fj && (fj < fi || (fj == fi && j < i));
+        rank += fj && (fj < fi || (fj == fi && j < tid));
       }
-      T.sorted[rank] = uint16_t(i);
+      T.sorted[rank] = uint16_t(tid);
+      atomicAdd(&T.nsym, 1u);
+      atomicAdd(&T.total, fi);
     }
   }
   __syncthreads();
-  if (tid == 0) {
-    uint32_t n = 0, total = 0;
-    for (int i = 0; i < 256; ++i) {
-      n += T.hist[i] > 0;
-      total += T.hist[i];
+  const int n = int(T.nsym);
+  const bool build = n >= 2 && T.total >= 256;
+  // Huffman tree by the two-queue method on the sorted leaves (serial):
+  // leaves 0 .. n-1 (ascending count), internal nodes n .. 2n-2 (root)
+  if (build && tid == 0) {
+    uint32_t* f = x.f;
+    int16_t* parent = x.parent;
+    for (int i = 0; i < n; ++i)
+      f[i] = T.hist[T.sorted[i]];
+    int leaf = 0, inode = n, next = n;
+    for (int k = 0; k < n - 1; ++k) {
+      int pick[2];
+      for (int t = 0; t < 2; ++t) {
+        if (leaf < n && (inode >= next || f[leaf] <= f[inode]))
+          pick[t] = leaf++;
+        else
+          pick[t] = inode++;
+      }
+      f[next] = f[pick[0]] + f[pick[1]];
+      parent[pick[0]] = parent[pick[1]] = int16_t(next);
+      ++next;
     }
-    T.nsym = n;
-    T.ok = 0;
-    if (total >= 256 && huff_lengths(T.hist, T.sorted, int(n), T.huff, T.hx)) {
-      huff_codes(T.huff, T.hx.rank_start, T.hx.count_w);
-      T.ok = huff_describe(T.huff, T.hx, T.tw) ? 1 : 0;
+    parent[2 * n - 2] = int16_t(2 * n - 2); // the root is its own parent
+  }
+  __syncthreads();
+  if (!build) {
+    if (tid == 0)
+      T.ok = 0;
+  } else {
+    // leaf depths by pointer jumping (depth <= 255 < 2^8)
+    const int nodes = 2 * n - 1;
+    uint8_t* dist = x.depth;
+    for (int i = tid; i < nodes; i += blockDim.x)
+      dist[i] = i == nodes - 1 ? 0 : 1;
+    __syncthreads();
+    for (int r = 0; r < 8; ++r) {
+      int16_t np[2];
+      uint8_t nd[2];
+      for (int k = 0; k < 2; ++k) {
+        const int i = tid + k * int(blockDim.x);
+        if (i < nodes) {
+          const int p = x.parent[i];
+          nd[k] = uint8_t(dist[i] + dist[p]);
+          np[k] = x.parent[p];
+        }
+      }
+      __syncthreads();
+      for (int k = 0; k < 2; ++k) {
+        const int i = tid + k * int(blockDim.x);
+        if (i < nodes) {
+          dist[i] = nd[k];
+          x.parent[i] = np[k];
+        }
+      }
+      __syncthreads();
     }
+    // lengths per depth, leaves deeper than kHufMaxBits clamped
+    if (tid < n) {
+      const uint32_t d = dist[tid];
+      atomicAdd(&x.count_w[d > kHufMaxBits ? kHufMaxBits : d], 1u);
+    }
+    __syncthreads();
+    if (tid == 0) {
+      // The clamped leaves overfill the code by `excess` units of
+      // 2^-kHufMaxBits.  Each step splits the deepest leaf above the limit
+      // into two leaves one level down, one of them taken from the limit
+      // (as zlib's gen_bitlen repairs its length counts): one unit less.
+      uint32_t* bl = x.count_w;
+      constexpr int M = int(kHufMaxBits);
+      uint32_t units = 0;
+      for (int L = 1; L <= M; ++L)
+        units += bl[L] << (M - L);
+      for (uint32_t excess = units - (1u << M); int(excess) > 0; --excess) {
+        int bits = M - 1;
+        while (bits > 0 && bl[bits] == 0)
+          --bits;
+        if (bits == 0 || bl[M] == 0)
+          break;
+        bl[bits]--;
+        bl[bits + 1] += 2;
+        bl[M]--;
+      }
+      int mb = 0;
+      uint32_t kraft = 0;
+      for (int L = 1; L <= int(kHufMaxBits); ++L)
+        if (bl[L])
+          mb = L;
+      for (int L = 1; L <= mb; ++L)
+        kraft += bl[L] << (mb - L);
+      h.max_bits = mb;
+      T.ok = kraft == (1u << mb) && bl[0] == 0 ? 1 : 0;
+      // rank_start[w]: canonical start of weight w = mb + 1 - length
+      uint32_t acc = 0;
+      for (int w = 1; w <= mb; ++w) {
+        x.rank_start[w] = acc;
+        acc += bl[mb + 1 - w] << (w - 1);
+      }
+    }
+    __syncthreads();
+    // the least frequent symbols get the longest codes
+    if (T.ok && tid < n) {
+      uint32_t cum = 0;
+      int L = int(kHufMaxBits);
+      for (; L > 0; --L) {
+        cum += x.count_w[L];
+        if (uint32_t(tid) < cum)
+          break;
+      }
+      h.len[T.sorted[tid]] = uint8_t(L);
+    }
+    __syncthreads();
+    // canonical codes in zstd's order: by weight, then by symbol
+    const int mb = h.max_bits;
+    const int sym = tid; // < 256
+    const int len = sym < 256 ? h.len[sym] : 0;
+    const int wt = len ? mb + 1 - len : 0;
+    uint32_t* cnt = x.f; // [warps][16] counts per weight
+    uint32_t below = 0;
+    for (int w = 1; w <= mb; ++w) {
+      const unsigned m = __ballot_sync(0xffffffffu, wt == w);
+      if (wt == w)
+        below = __popc(m & ((1u << lane) - 1));
+      if (lane == 0)
+        cnt[warp * 16 + w] = __popc(m);
+    }
+    __syncthreads();
+    if (sym < 256 && len > 0) {
+      for (int v = 0; v < warp; ++v)
+        below += cnt[v * 16 + wt];
+      h.code[sym] = uint16_t((x.rank_start[wt] >> (wt - 1)) + below);
+    }
+    // the highest coded symbol; weights of the symbols below it
+    if (tid == 0)
+      h.last = 0;
+    __syncthreads();
+    if (sym < 256 && len > 0)
+      atomicMax(&h.last, sym);
+    // (h.last is read after the barrier below)
+    __syncthreads();
+    if (sym < h.last)
+      x.w[sym] = uint8_t(wt);
+    __syncthreads();
+    if (tid == 0 && T.ok)
+      T.ok = huff_describe(h, x, T.tw) ? 1 : 0;
   }
   __syncthreads();
   ChunkTable& ct = tables[chunk];
-  for (int c = tid; c < 256; c += blockDim.x)
-    ct.cl[c] = T.ok ? uint32_t(T.huff.code[c]) | (uint32_t(T.huff.len[c]) << 16) : 0;
-  const int dl = T.ok ? T.huff.desc_len : 0;
+  if (tid < 256)
+    ct.cl[tid] = T.ok ? uint32_t(h.code[tid]) | (uint32_t(h.len[tid]) << 16) : 0;
+  const int dl = T.ok ? h.desc_len : 0;
   for (int i = tid; i < dl; i += blockDim.x)
-    ct.desc[i] = T.huff.desc[i];
+    ct.desc[i] = h.desc[i];
   if (tid == 0) {
     ct.desc_len = uint32_t(dl);
     ct.ok = T.ok;
@@ -923,6 +976,7 @@ zstd_block_k(CodecBatch b,
     }
     S.all_same = all_same;
     S.lit_same = lit_same;
+    S.lit_missing = 0;
     S.seq_bad = 0;
   }
   __syncthreads();
@@ -956,10 +1010,30 @@ zstd_block_k(CodecBatch b,
     // this thread's share of the stream in writing order (reversed)
     const uint32_t q0 = uint32_t(uint64_t(m) * t / kStreamThreads);
     const uint32_t q1 = uint32_t(uint64_t(m) * (t + 1) / kStreamThreads);
-    uint32_t bits = 0;
+    uint32_t bits = 0, missing = 0; // missing: a literal without a code
     const uint32_t* cl = S.cl;
-    for_each_desc(lits, a1 - q1, a1 - q0,
-                  [&](uint8_t c) { bits += cl[c] >> 16; });
+    visit_desc(
+      lits, a1 - q1, a1 - q0,
+      [&](uint8_t c) {
+        const uint32_t L = cl[c] >> 16;
+        bits += L;
+        missing |= L == 0;
+      },
+      [&](const uint4& w) {
+        uint32_t s4[4] = { 0, 0, 0, 0 };
+        const uint32_t v[4] = { w.x, w.y, w.z, w.w };
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+          for (int k = 0; k < 4; ++k) {
+            const uint32_t L = cl[(v[i] >> (8 * k)) & 255] >> 16;
+            s4[i] += L;
+            missing |= L == 0;
+          }
+        bits += s4[0] + s4[1] + s4[2] + s4[3];
+      });
+    if (missing) // the chunk's table does not cover these literals
+      S.lit_missing = 1;
     // exclusive scan over the stream's threads (whole warps)
     uint32_t before = bits;
     for (int o = 1; o < 32; o <<= 1) {
@@ -999,7 +1073,7 @@ zstd_block_k(CodecBatch b,
         S.stream_pos[s] = pos;
         pos += ssz[s];
       }
-      if (csize + hdr >= nlit + 3) // not worth it
+      if (csize + hdr >= nlit + 3 || S.lit_missing) // not worth it / no code
         S.lit_mode = 0;
       else {
         uint8_t* o = stage + 3;
@@ -1041,10 +1115,7 @@ zstd_block_k(CodecBatch b,
       bool first = true;
       uint64_t acc = 0;
       const uint32_t* cl = S.cl;
-      for_each_desc(lits, a1 - q1, a1 - q0, [&](uint8_t c) {
-        const uint32_t e = cl[c];
-        acc |= uint64_t(e & 0xFFFF) << fill;
-        fill += int(e >> 16);
+      auto flush = [&]() {
         if (fill >= 32) {
           if (first && first_shared)
             atomicOr(wbase + word, uint32_t(acc));
@@ -1055,7 +1126,30 @@ zstd_block_k(CodecBatch b,
           fill -= 32;
           ++word;
         }
-      });
+      };
+      // codes are at most 11 bits: two fit before a flush (fill < 54)
+      auto put = [&](uint32_t e) {
+        acc |= uint64_t(e & 0xFFFF) << fill;
+        fill += int(e >> 16);
+      };
+      visit_desc(
+        lits, a1 - q1, a1 - q0,
+        [&](uint8_t c) {
+          put(cl[c]);
+          flush();
+        },
+        [&](const uint4& w) {
+          const uint32_t v[4] = { w.w, w.z, w.y, w.x };
+#pragma unroll
+          for (int i = 0; i < 4; ++i) {
+            put(cl[v[i] >> 24]);
+            put(cl[(v[i] >> 16) & 255]);
+            flush();
+            put(cl[(v[i] >> 8) & 255]);
+            put(cl[v[i] & 255]);
+            flush();
+          }
+        });
       if (t == kStreamThreads - 1) { // end mark after the stream's last bit
         acc |= uint64_t(1) << fill;
         fill += 1;
@@ -1234,46 +1328,58 @@ zstd_block_k(CodecBatch b,
 // frame: header + blocks
 // ---------------------------------------------------------------------------
 
+// Frame header size for a chunk of n bytes (single segment, content size).
+__device__ __forceinline__ uint32_t frame_header_bytes(uint32_t n)
+{
+  return n < 256 ? 6 : (n < 65536 + 256 ? 7 : 9);
+}
+
+// One CTA per block: place the block at its offset in the chunk's frame
+// (header + the sizes of the blocks before it); block 0 also writes the
+// frame header and the last block the chunk's compressed size.
 __global__ void __launch_bounds__(256)
 zstd_frame_k(CodecBatch b,
              const uint8_t* stage_all,
              const uint32_t* block_sizes,
              uint32_t blocks_per_chunk)
 {
-  __shared__ uint32_t offs[1024];
-  const uint64_t chunk = blockIdx.x;
+  __shared__ uint32_t off;
+  const uint64_t blk = blockIdx.x;
+  const uint64_t chunk = blk / blocks_per_chunk;
+  const uint32_t k = uint32_t(blk % blocks_per_chunk);
   uint8_t* out = b.out + b.id(chunk) * b.out_stride;
   const uint32_t n = b.chunk_bytes;
-  if (threadIdx.x == 0) {
-    // magic, descriptor (single segment), frame content size
-    put_le(out, 0xFD2FB528u, 4);
-    uint32_t h;
-    if (n < 256) {
-      out[4] = 0x20; // FCS flag 0, single segment
-      out[5] = uint8_t(n);
-      h = 6;
-    } else if (n < 65536 + 256) {
-      out[4] = 0x60; // FCS flag 1 (2 bytes, value - 256)
-      put_le(out + 5, n - 256, 2);
-      h = 7;
-    } else {
-      out[4] = 0xA0; // FCS flag 2 (4 bytes)
-      put_le(out + 5, n, 4);
-      h = 9;
+  const uint32_t* sizes = block_sizes + chunk * blocks_per_chunk;
+  if (threadIdx.x < 32) {
+    const unsigned lane = threadIdx.x;
+    uint32_t acc = 0;
+    for (uint32_t i = lane; i < k; i += 32)
+      acc += sizes[i];
+    for (int o = 16; o; o >>= 1)
+      acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) {
+      const uint32_t h = frame_header_bytes(n);
+      off = h + acc;
+      if (k == 0) { // magic, descriptor (single segment), frame content size
+        put_le(out, 0xFD2FB528u, 4);
+        if (h == 6) {
+          out[4] = 0x20; // FCS flag 0
+          out[5] = uint8_t(n);
+        } else if (h == 7) {
+          out[4] = 0x60; // FCS flag 1 (2 bytes, value - 256)
+          put_le(out + 5, n - 256, 2);
+        } else {
+          out[4] = 0xA0; // FCS flag 2 (4 bytes)
+          put_le(out + 5, n, 4);
+        }
+      }
+      if (k + 1 == blocks_per_chunk)
+        b.out_sizes[b.id(chunk)] = h + acc + sizes[k];
     }
-    uint32_t acc = h;
-    for (uint32_t k = 0; k < blocks_per_chunk && k < 1024; ++k) {
-      offs[k] = acc;
-      acc += block_sizes[chunk * blocks_per_chunk + k];
-    }
-    b.out_sizes[b.id(chunk)] = acc;
   }
   __syncthreads();
-  for (uint32_t k = 0; k < blocks_per_chunk; ++k) {
-    const uint8_t* src = stage_all + (chunk * blocks_per_chunk + k) * kStageBytes;
-    const uint32_t sz = block_sizes[chunk * blocks_per_chunk + k];
-    copy_bytes(out + offs[k], src, sz, threadIdx.x, blockDim.x);
-  }
+  copy_bytes(out + off, stage_all + blk * kStageBytes, sizes[k], threadIdx.x,
+             blockDim.x);
 }
 
 } // namespace
@@ -1294,8 +1400,6 @@ cudaError_t launch_zstd(CodecBatch b, void* scratch, cudaStream_t st)
     return cudaSuccess;
   b.segs_per_chunk = (b.chunk_bytes + kSegBytes - 1) / kSegBytes;
   const uint32_t bpc = (b.chunk_bytes + kBlockBytes - 1) / kBlockBytes;
-  if (bpc > 1024)
-    return cudaErrorInvalidValue; // chunks above 128 MiB
   const uint64_t segs = b.n_chunks * b.segs_per_chunk;
   const uint64_t blocks = b.n_chunks * bpc;
   uint8_t* p = static_cast<uint8_t*>(scratch);
@@ -1341,7 +1445,7 @@ cudaError_t launch_zstd(CodecBatch b, void* scratch, cudaStream_t st)
                 pre, seqs, meta, tables, litbuf, stage, bsizes, bpc);
   if ((e = cudaGetLastError()) != cudaSuccess)
     return e;
-  CHUCKY_LAUNCH(zstd_frame_k, unsigned(b.n_chunks), 256, 0, st, b, stage, bsizes, bpc);
+  CHUCKY_LAUNCH(zstd_frame_k, unsigned(blocks), 256, 0, st, b, stage, bsizes, bpc);
   return cudaGetLastError();
 }
 

@@ -191,6 +191,14 @@ inline unsigned atomicOr(unsigned* p, unsigned v)
     simt::fail("misaligned 32-bit atomicOr");
   return std::atomic_ref<unsigned>(*p).fetch_or(v);
 }
+inline int atomicMax(int* p, int v)
+{
+  std::atomic_ref<int> a(*p);
+  int cur = a.load();
+  while (cur < v && !a.compare_exchange_weak(cur, v)) {
+  }
+  return cur;
+}
 inline unsigned atomicAnd(unsigned* p, unsigned v)
 {
   if (reinterpret_cast<uintptr_t>(p) & 3)

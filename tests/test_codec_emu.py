@@ -35,7 +35,9 @@ def emu():
 
 CASES = [(1024, 6), (37, 3), (13, 2), (1, 2)]
 BIG = [("zstd", "xor16", 200000, 1), ("zstd", "mixed", 131072, 2),
-       ("lz4", "xor16", 140000, 1), ("lz4", "mixed", 65536, 2)]
+       ("lz4", "xor16", 140000, 1), ("lz4", "mixed", 65536, 2),
+       # skewed bytes: Huffman depths beyond the 11-bit limit get repaired
+       ("zstd", "geom", 40000, 1), ("lz4", "geom", 9000, 1)]
 
 
 def _run(emu, codec, pattern, chunk, n):
