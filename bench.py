@@ -116,6 +116,23 @@ class Clocks:
                 "samples": len(self.samples)}
 
 
+def max_over_ranks(values, world, device):
+    """Element-wise maximum of per-rank timings over all ranks (replicas:
+    the job takes as long as its slowest rank)."""
+    if world <= 1:
+        return list(values)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor(values, dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(v) for v in t.tolist()]
+
+
+def whole_job_gbs(bytes_per_rank_step, steps, world, ms):
+    """Input GB/s of the whole job: every rank ingests its own replica."""
+    return bytes_per_rank_step * steps * world / (ms * 1e-3) / 1e9
+
+
 def run_ours(args, rank, world):
     import torch
     import chucky_gb300 as cg
@@ -195,16 +212,9 @@ def run_ours(args, rank, world):
     times_host, _, _, sink_h, launches_h = timed(host, args.steps, max(1, args.warmup // 2))
     clk = clocks.stop() if rank == 0 else None
 
-    ms_dev = float(np.sum(times_dev))
-    ms_host = float(np.sum(times_host))
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms_dev, ms_host], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_dev, ms_host = float(t[0]), float(t[1])
-    total = nbytes * args.steps * world
-    value = total / (ms_dev * 1e-3) / 1e9
-    e2e = total / (ms_host * 1e-3) / 1e9
+    ms_dev, ms_host = max_over_ranks([float(np.sum(times_dev)), float(np.sum(times_host))],
+                                     world, dev)
+    value, e2e = (whole_job_gbs(nbytes, args.steps, world, ms) for ms in (ms_dev, ms_host))
 
     # dominant kernel: the zstd encoder (find + block + frame launches),
     # event-timed on its own stream inside the library

@@ -5,10 +5,10 @@
 // threads stage the region's bytes in shared memory (lz77_stage_region),
 // then warp w parses segment w of the region with a private hash table
 // (kHashLog-bit hash of 4 bytes -> last position, 16-bit positions relative
-// to the region).  Before parsing, a warp enters every position of the
-// region that precedes its segment into its table (insert only), so its
-// matches may reach back to the start of the region, as a single parse of
-// the region would; the segments are parsed side by side.
+// to the region).  Before parsing, a warp enters the positions of the
+// kHistorySegs segments of the region before its own into its table
+// (insert only), so its matches may reach back into them, as a single
+// sequential parse would; the segments are parsed side by side.
 //
 // The segment is scanned in windows of 32 positions, one per lane (with a
 // stride that grows by one for every 2^kSearchStrength literals since the
@@ -22,8 +22,8 @@
 // times as the window allows; a match that reaches kLaneExtend bytes is
 // extended by the whole warp, 32 bytes per step.  Windows inside a long
 // match are skipped.  Matches end inside their segment and start inside
-// their region.  (When lanes of one window share a hash slot the hardware
-// keeps one of their stores.)
+// it or its history.  (When lanes of one window share a hash slot the
+// hardware keeps one of their stores.)
 //
 // Output per segment: sequences (literal length, match length, offset) in
 // scratch, the sequence count and the trailing literal count.
@@ -49,7 +49,7 @@ constexpr uint32_t kLaneExtend = 64;
 #define CHUCKY_SEARCH_STRENGTH 8
 #endif
 #ifndef CHUCKY_HISTORY_SEGS
-#define CHUCKY_HISTORY_SEGS 3
+#define CHUCKY_HISTORY_SEGS 1
 #endif
 // positions probed per lane step grow by one for every 2^kSearchStrength
 // literals since the last match (sparse probing of incompressible runs)

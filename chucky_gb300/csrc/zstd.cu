@@ -746,22 +746,36 @@ zstd_table_k(const uint32_t* chunk_hist, ChunkTable* tables)
   const bool build = n >= 2 && T.total >= 256;
   // Huffman tree by the two-queue method on the sorted leaves (serial):
   // leaves 0 .. n-1 (ascending count), internal nodes n .. 2n-2 (root)
+  if (build && tid < n)
+    x.f[tid] = T.hist[T.sorted[tid]];
+  __syncthreads();
   if (build && tid == 0) {
     uint32_t* f = x.f;
     int16_t* parent = x.parent;
-    for (int i = 0; i < n; ++i)
-      f[i] = T.hist[T.sorted[i]];
+    // the heads of both queues stay in registers (empty: ~0u)
     int leaf = 0, inode = n, next = n;
+    uint32_t fl = f[0], fi = ~0u;
     for (int k = 0; k < n - 1; ++k) {
       int pick[2];
+      uint32_t val[2];
       for (int t = 0; t < 2; ++t) {
-        if (leaf < n && (inode >= next || f[leaf] <= f[inode]))
-          pick[t] = leaf++;
-        else
-          pick[t] = inode++;
+        if (fl <= fi) { // ties take the leaf
+          pick[t] = leaf;
+          val[t] = fl;
+          ++leaf;
+          fl = leaf < n ? f[leaf] : ~0u;
+        } else {
+          pick[t] = inode;
+          val[t] = fi;
+          ++inode;
+          fi = inode < next ? f[inode] : ~0u;
+        }
       }
-      f[next] = f[pick[0]] + f[pick[1]];
+      const uint32_t sum = val[0] + val[1];
+      f[next] = sum;
       parent[pick[0]] = parent[pick[1]] = int16_t(next);
+      if (inode == next) // the internal queue was empty: this node heads it
+        fi = sum;
       ++next;
     }
     parent[2 * n - 2] = int16_t(2 * n - 2); // the root is its own parent
@@ -900,7 +914,7 @@ zstd_table_k(const uint32_t* chunk_hist, ChunkTable* tables)
   }
 }
 
-__global__ void __launch_bounds__(kBlockThreads)
+__global__ void __launch_bounds__(kBlockThreads, 4)
 zstd_block_k(CodecBatch b,
              const __grid_constant__ PredefTables pre,
              const Seq* seqs,
@@ -1082,22 +1096,29 @@ zstd_block_k(CodecBatch b,
         const uint64_t h = 2u | (sf << 2) | (uint64_t(nlit) << 4) |
                            (uint64_t(csize) << (4 + nbits));
         put_le(o, h, hdr);
-        o += hdr;
-        for (uint32_t i = 0; i < dlen; ++i)
-          o[i] = ct.desc[i];
-        o += dlen;
+        o += hdr + dlen; // the description is copied by all threads below
         put_le(o, ssz[0], 2);
         put_le(o + 2, ssz[1], 2);
         put_le(o + 4, ssz[2], 2);
       }
     }
-    // zero the stream area before the bit packing ORs into it
+    // copy the tree description; zero the stream area before the bit
+    // packing ORs into it (16-byte stores between byte-wise ends)
     __syncthreads();
     if (S.lit_mode == 2) {
+      const uint32_t dlen = ct.desc_len;
+      for (uint32_t i = tid; i < dlen; i += blockDim.x)
+        stage[3 + S.lit_hdr + i] = ct.desc[i];
       const uint32_t z0 = S.stream_pos[0];
-      const uint32_t z1 = S.lit_size + 3;
-      for (uint32_t i = z0 + tid; i < z1 + 4; i += blockDim.x)
-        stage[i] = 0;
+      const uint32_t z1 = S.lit_size + 3 + 4;
+      const uint32_t v0 = min(z1, (z0 + 15) & ~15u), v1 = max(v0, z1 & ~15u);
+      if (tid < v0 - z0)
+        stage[z0 + tid] = 0;
+      if (tid < z1 - v1)
+        stage[v1 + tid] = 0;
+      uint4* zv = reinterpret_cast<uint4*>(stage + v0);
+      for (uint32_t i = tid; i < (v1 - v0) / 16; i += blockDim.x)
+        zv[i] = make_uint4(0, 0, 0, 0);
     }
     __syncthreads();
     if (S.lit_mode == 2) {
@@ -1279,8 +1300,15 @@ zstd_block_k(CodecBatch b,
       if (nseq)
         *o = 0; // predefined LL, OF and ML tables
     }
-    for (uint32_t i = bs0 + tid; i < bs0 + nbytes + 4; i += blockDim.x)
-      stage[i] = 0;
+    const uint32_t z1 = bs0 + nbytes + 4;
+    const uint32_t v0 = min(z1, (bs0 + 15) & ~15u), v1 = max(v0, z1 & ~15u);
+    if (tid < v0 - bs0)
+      stage[bs0 + tid] = 0;
+    if (tid < z1 - v1)
+      stage[v1 + tid] = 0;
+    uint4* zv = reinterpret_cast<uint4*>(stage + v0);
+    for (uint32_t i = tid; i < (v1 - v0) / 16; i += blockDim.x)
+      zv[i] = make_uint4(0, 0, 0, 0);
   }
   __syncthreads();
   if (fits && nseq) {
