@@ -83,10 +83,15 @@ class Clocks:
                  "clocks_event_reasons.hw_thermal_slowdown,"
                  "clocks_event_reasons.sw_thermal_slowdown,"
                  "clocks_event_reasons.sw_power_cap",
-                 "--format=csv,noheader,nounits", "-lms", "100", "-i",
+                 "--format=csv,noheader,nounits", "-lms", "20", "-i",
                  os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0] or "0"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             threading.Thread(target=self._read, daemon=True).start()
+            # the timed region starts once samples flow
+            t0 = time.time()
+            while not self.samples and time.time() - t0 < 5:
+                time.sleep(0.01)
+            self.samples.clear()
         except Exception:
             self.proc = None
 

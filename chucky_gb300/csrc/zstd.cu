@@ -29,14 +29,25 @@ namespace {
 
 // 32 KiB blocks: every block builds its own Huffman table serially, so
 // smaller blocks put more of them in flight (the table costs ~0.3% ratio)
-constexpr uint32_t kBlockLog = 15;
-constexpr uint32_t kBlockBytes = 1u << kBlockLog; // 32 KiB
+constexpr uint32_t kBlockLog = 13;
+constexpr uint32_t kBlockBytes = 1u << kBlockLog; // 8 KiB
 constexpr uint32_t kSegsPerBlock = kBlockBytes / kSegBytes;
-constexpr uint32_t kStageBytes = kBlockBytes + 1024;
-constexpr int kStreamThreads = 64;                // two warps per Huffman stream
+// staging of one compressed block: a block that carries its chunk's
+// Huffman description is never replaced by a raw block, so it must fit
+// however large it comes out (literals <= 11/8 of their bytes, sequences
+// <= 9 bytes each)
+constexpr uint32_t kStageBytes = 3 * kBlockBytes + 1024;
+constexpr int kStreamThreads = 32;                // a warp per Huffman stream
 constexpr int kBlockThreads = 4 * kStreamThreads; // >= a warp per segment
+constexpr int kTableThreads = 256;                // a thread per symbol
 static_assert(kBlockThreads >= 32 * int(kSegsPerBlock), "warp per segment");
 static_assert(kStreamThreads % 32 == 0, "whole warps per stream");
+// fewest literals coded with the chunk's Huffman table
+constexpr uint32_t kMinHufLits = 64;
+// chunks at least this large share one Huffman description: the first
+// block that codes literals with it carries it, later blocks refer to it
+// (treeless literals); smaller chunks describe the table in every block
+constexpr uint32_t kTreelessMinChunk = 64u << 10;
 constexpr uint32_t kHufMaxBits = 11;
 #ifndef CHUCKY_ZSTD_MIN_MATCH
 #define CHUCKY_ZSTD_MIN_MATCH 6
@@ -50,42 +61,6 @@ struct ZSeg
   // bits 0-7 first literal byte, bit 8 every literal equals it (or none);
   // bits 16-23 first input byte, bit 24 every input byte equals it
   uint32_t flags;
-};
-
-// ---------------------------------------------------------------------------
-// bit writer for backward-read streams (written forward, LSB first; the
-// decoder starts at the highest set bit of the last byte)
-// ---------------------------------------------------------------------------
-
-struct BitOut
-{
-  uint8_t* p;
-  uint64_t acc;
-  int n;
-  __device__ void init(uint8_t* dst)
-  {
-    p = dst;
-    acc = 0;
-    n = 0;
-  }
-  __device__ __forceinline__ void put(uint64_t v, int bits)
-  {
-    acc |= (v & ((uint64_t(1) << bits) - 1)) << n;
-    n += bits;
-    while (n >= 8) {
-      *p++ = uint8_t(acc);
-      acc >>= 8;
-      n -= 8;
-    }
-  }
-  // end mark + padding; returns one past the last byte written
-  __device__ uint8_t* close()
-  {
-    put(1, 1);
-    if (n > 0)
-      *p++ = uint8_t(acc);
-    return p;
-  }
 };
 
 // ---------------------------------------------------------------------------
@@ -155,21 +130,6 @@ struct PredefTables
 {
   FseEnc ll, ml, of;
 };
-
-// v in [size, 2 size): emit bits, move to a state of symbol s.
-__device__ __forceinline__ void fse_encode(const FseEnc& t,
-                                           uint32_t& v,
-                                           int s,
-                                           BitOut& bo)
-{
-  const int c = t.count[s], h = highbit(uint32_t(c));
-  int nb = t.al - h;
-  if ((v >> nb) < uint32_t(c))
-    --nb;
-  bo.put(v, nb);
-  const uint32_t x = v >> nb;
-  v = t.states[t.first[s] + (x - c)] + (1u << t.al);
-}
 
 __device__ __forceinline__ uint32_t fse_init(const FseEnc& t, int s)
 {
@@ -436,63 +396,13 @@ __device__ int write_ncount(uint8_t* out, const int16_t* norm, int nsym, int al)
   return len;
 }
 
-// Tree description: direct 4-bit weights when <= 128 weights, else FSE.
-// x.w holds the weights of symbols 0 .. h.last - 1.
-__device__ bool huff_describe(Huff& h, HuffScratch& x, FseEnc& t)
+// FSE bookkeeping of the weights description (the state chain runs on one
+// thread; the bits are then packed by all threads).
+struct WeightChain
 {
-  const int nw = h.last; // explicit weights: symbols < last (in x.w)
-  const uint8_t* w = x.w;
-  if (nw <= 128) {
-    h.desc[0] = uint8_t(127 + nw);
-    for (int i = 0; i < (nw + 1) / 2; ++i) {
-      const uint8_t hi = w[2 * i], lo = 2 * i + 1 < nw ? w[2 * i + 1] : 0;
-      h.desc[1 + i] = uint8_t(hi << 4 | lo);
-    }
-    h.desc_len = 1 + (nw + 1) / 2;
-    return true;
-  }
-  // FSE-compressed weights, accuracy log 6, two interleaved states
-  uint32_t* hist = x.whist;
-  for (int i = 0; i < 16; ++i)
-    hist[i] = 0;
-  int maxw = 0;
-  for (int s = 0; s < nw; ++s) {
-    hist[w[s]]++;
-    maxw = w[s] > maxw ? w[s] : maxw;
-  }
-  const int nsym = maxw + 2 <= 13 ? maxw + 2 : 13; // room for a spare symbol
-  int16_t* norm = x.norm;
-  const int al = 6;
-  norm_weights(hist, nsym, al, norm);
-  fse_build(t, norm, nsym, al, x.spread, x.fill);
-  uint8_t* out = h.desc + 1;
-  int len = write_ncount(out, norm, nsym, al);
-  BitOut bo;
-  bo.init(out + len);
-  uint32_t v1, v2;
-  int i = nw;
-  if (nw & 1) {
-    v1 = fse_init(t, w[--i]);
-    v2 = fse_init(t, w[--i]);
-    fse_encode(t, v1, w[--i], bo);
-  } else {
-    v2 = fse_init(t, w[--i]);
-    v1 = fse_init(t, w[--i]);
-  }
-  while (i > 0) {
-    fse_encode(t, v2, w[--i], bo);
-    fse_encode(t, v1, w[--i], bo);
-  }
-  bo.put(v2 - (1u << al), al);
-  bo.put(v1 - (1u << al), al);
-  const uint8_t* end = bo.close();
-  len = int(end - out);
-  if (len >= 128)
-    return false;
-  h.desc[0] = uint8_t(len);
-  h.desc_len = 1 + len;
-  return true;
-}
+  uint16_t enc[256]; // per step: low bits | bit count << 8
+  uint32_t nsteps, ncount_len, fin1, fin2, maxw, warp_bits[8];
+};
 
 // ---------------------------------------------------------------------------
 // block
@@ -505,8 +415,45 @@ struct ChunkTable
   uint32_t cl[256];    // code | length << 16; 0 for absent symbols
   uint8_t desc[320];   // tree description (header byte + payload)
   uint32_t desc_len;
-  uint32_t ok;         // a usable table exists
+  uint32_t ok;         // a usable table exists and beats raw literals
+  uint32_t carrier;    // block carrying the description (treeless chunks);
+                       // ~0u: every Huffman block carries it
 };
+
+// Literal count and single-valuedness of block `bi` of a chunk from its
+// segments' metadata.
+__device__ __forceinline__ void block_literals(const ZSeg* meta,
+                                               uint64_t seg_first,
+                                               uint32_t chunk_bytes,
+                                               uint32_t bi,
+                                               uint32_t& nlit,
+                                               bool& same)
+{
+  const uint32_t b0 = bi * kBlockBytes;
+  const uint32_t b1 = min(chunk_bytes, b0 + kBlockBytes);
+  const uint32_t nsegs = (b1 - b0 + kSegBytes - 1) / kSegBytes;
+  const uint64_t sb = seg_first + b0 / kSegBytes;
+  nlit = 0;
+  same = true;
+  int byte = -1;
+  for (uint32_t k = 0; k < nsegs; ++k) {
+    const ZSeg m = meta[sb + k];
+    const uint32_t s0 = b0 + k * kSegBytes;
+    const uint32_t nl = min(b1, s0 + kSegBytes) - s0 - m.matched;
+    nlit += nl;
+    if (nl) {
+      if (byte < 0)
+        byte = int(m.flags & 0xFF);
+      same &= ((m.flags >> 8) & 1) && (m.flags & 0xFF) == uint32_t(byte);
+    }
+  }
+}
+
+// Whether block literals are coded with the chunk's Huffman table.
+__device__ __forceinline__ bool block_uses_table(bool table_ok, uint32_t nlit, bool same)
+{
+  return table_ok && !same && nlit >= kMinHufLits;
+}
 
 struct TableShared
 {
@@ -514,6 +461,9 @@ struct TableShared
   uint16_t sorted[256]; // used symbols by (count, symbol)
   uint32_t nsym, total;
   uint32_t ok;
+  unsigned long long bits; // coded size of the chunk's literals
+  uint32_t carrier;
+  WeightChain wc;
   FseEnc tw;            // Huffman weights table
   HuffScratch hx;
   Huff huff;
@@ -535,6 +485,8 @@ struct BlockShared
   uint32_t lit_size;      // literals section bytes (header included)
   uint32_t lit_same;      // every literal equals the first
   uint32_t lit_missing;   // a literal has no code in the chunk's table
+  uint32_t with_desc;     // the literals section describes the table
+  uint32_t forced;        // description carrier: never a raw block
   uint32_t all_same;
   // sequences section
   uint32_t ll_base[36], ml_base[53];
@@ -551,10 +503,12 @@ __device__ __forceinline__ void put_le(uint8_t* p, uint64_t v, int n)
     p[i] = uint8_t(v >> (8 * i));
 }
 
-// Bit packing into a stream shared by many threads: each thread owns a
-// contiguous bit range [start, start + n) of the stream at `p` (zeroed
-// beforehand).  Words wholly inside the range are stored plainly; the first
-// (shared with the bytes or thread before) and the last are OR-ed in.
+// Bit packing into a stream shared by many threads (zstd's backward-read
+// bitstreams are written forward, least significant bit first; the decoder
+// starts at the end mark).  Each thread owns a contiguous bit range
+// [start, start + n) of the stream at `p` (zeroed beforehand).  Words
+// wholly inside the range are stored plainly; the first (shared with the
+// bytes or thread before) and the last are OR-ed in.
 struct BitPack
 {
   uint32_t* w;
@@ -709,10 +663,132 @@ __device__ __forceinline__ void visit_desc(const uint8_t* lits,
 // One CTA per chunk: the length-limited Huffman code of the chunk's
 // literal histogram and its tree description (thread 0 builds, the rest
 // rank the symbols and publish the table).
-__global__ void __launch_bounds__(kBlockThreads)
-zstd_table_k(const uint32_t* chunk_hist, ChunkTable* tables)
+// Tree description (RFC 8878 4.2.1): direct 4-bit weights for up to 128
+// weights, else the weights FSE-compressed (accuracy log 6, two
+// interleaved states).  x.w holds the weights of symbols 0 .. h.last - 1.
+// All threads of the CTA call it; it sets T.ok to 0 when the description
+// does not fit.
+__device__ void huff_describe(TableShared& T, int tid)
 {
-  static_assert(kBlockThreads >= 256, "a thread per symbol");
+  Huff& h = T.huff;
+  HuffScratch& x = T.hx;
+  WeightChain& c = T.wc;
+  const int nw = h.last;
+  const uint8_t* w = x.w;
+  const int lane = tid & 31, warp = tid >> 5;
+  if (nw <= 128) {
+    if (tid < (nw + 1) / 2) {
+      const uint8_t hi = w[2 * tid], lo = 2 * tid + 1 < nw ? w[2 * tid + 1] : 0;
+      h.desc[1 + tid] = uint8_t(hi << 4 | lo);
+    }
+    if (tid == 0) {
+      h.desc[0] = uint8_t(127 + nw);
+      h.desc_len = 1 + (nw + 1) / 2;
+    }
+    __syncthreads();
+    return;
+  }
+  if (tid < 16)
+    x.whist[tid] = 0;
+  if (tid == 0)
+    c.maxw = 0;
+  __syncthreads();
+  if (tid < nw) {
+    atomicAdd(&x.whist[w[tid]], 1u);
+    atomicMax(&c.maxw, uint32_t(w[tid]));
+  }
+  __syncthreads();
+  constexpr int al = 6;
+  uint8_t* out = h.desc + 1;
+  if (tid == 0) {
+    const int nsym = int(c.maxw) + 2 <= 13 ? int(c.maxw) + 2 : 13; // room for a spare symbol
+    norm_weights(x.whist, nsym, al, x.norm);
+    fse_build(T.tw, x.norm, nsym, al, x.spread, x.fill);
+    c.ncount_len = uint32_t(write_ncount(out, x.norm, nsym, al));
+    // the two state chains, last weight first; record each step's bits
+    const FseEnc& t = T.tw;
+    uint32_t v1, v2;
+    int i = nw, k = 0;
+    auto step = [&](uint32_t& v, int s) {
+      const int cnt = t.count[s];
+      int nb = al - highbit(uint32_t(cnt));
+      if ((v >> nb) < uint32_t(cnt))
+        --nb;
+      c.enc[k++] = uint16_t((v & ((1u << nb) - 1)) | (uint32_t(nb) << 8));
+      v = t.states[t.first[s] + ((v >> nb) - cnt)] + (1u << al);
+    };
+    if (nw & 1) {
+      v1 = fse_init(t, w[--i]);
+      v2 = fse_init(t, w[--i]);
+      step(v1, w[--i]);
+    } else {
+      v2 = fse_init(t, w[--i]);
+      v1 = fse_init(t, w[--i]);
+    }
+    while (i > 0) {
+      step(v2, w[--i]);
+      step(v1, w[--i]);
+    }
+    c.nsteps = uint32_t(k);
+    c.fin1 = v1 - (1u << al);
+    c.fin2 = v2 - (1u << al);
+  }
+  __syncthreads();
+  // pack: thread k writes step k's bits at the sum of the steps before it
+  const uint32_t ns = c.nsteps, len = c.ncount_len;
+  const uint32_t e = uint32_t(tid) < ns ? c.enc[tid] : 0;
+  const uint32_t nb = e >> 8;
+  uint32_t before = nb;
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, before, o);
+    if (lane >= o)
+      before += y;
+  }
+  if (lane == 31)
+    c.warp_bits[warp] = before;
+  before -= nb;
+  for (uint32_t i = 1 + len + tid; i < sizeof(h.desc); i += blockDim.x)
+    h.desc[i] = 0;
+  __syncthreads();
+  uint32_t total = 0;
+  for (int v = 0; v < kTableThreads / 32; ++v) {
+    if (v < warp)
+      before += c.warp_bits[v];
+    total += c.warp_bits[v];
+  }
+  const uint32_t bytes = (total + 2 * al + 1 + 7) / 8;
+  const bool fits = 1 + len + bytes + 4 <= sizeof(h.desc) && len + bytes < 128;
+  if (fits && (uint32_t(tid) < ns || (ns == 0 && tid == 0))) {
+    BitPack bp;
+    bp.init(out + len, before);
+    bp.put(e & 0xFF, int(nb));
+    if (uint32_t(tid) + 1 == ns || ns == 0) { // final states, end mark
+      bp.put(c.fin2, al);
+      bp.put(c.fin1, al);
+      bp.put(1, 1);
+    }
+    bp.flush();
+  }
+  __syncthreads();
+  if (tid == 0) {
+    if (fits) {
+      h.desc[0] = uint8_t(len + bytes);
+      h.desc_len = int(1 + len + bytes);
+    } else {
+      T.ok = 0;
+    }
+  }
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(kTableThreads)
+zstd_table_k(CodecBatch b,
+             const uint32_t* chunk_hist,
+             const ZSeg* meta,
+             ChunkTable* tables,
+             uint32_t blocks_per_chunk)
+{
+  static_assert(kTableThreads >= 256, "a thread per symbol");
   __shared__ TableShared T;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const uint64_t chunk = blockIdx.x;
@@ -898,8 +974,32 @@ zstd_table_k(const uint32_t* chunk_hist, ChunkTable* tables)
     if (sym < h.last)
       x.w[sym] = uint8_t(wt);
     __syncthreads();
+    if (T.ok)
+      huff_describe(T, tid);
+    // worth it: the coded literals (and one description) beat raw bytes
+    if (tid == 0)
+      T.bits = 0;
+    __syncthreads();
+    if (T.ok && sym < 256 && len > 0)
+      atomicAdd(&T.bits, (unsigned long long)T.hist[sym] * uint32_t(len));
+    __syncthreads();
     if (tid == 0 && T.ok)
-      T.ok = huff_describe(h, x, T.tw) ? 1 : 0;
+      T.ok = T.bits / 8 + uint32_t(h.desc_len) + 16 < uint64_t(T.total);
+  }
+  // the description carrier: the chunk's first block coding its literals
+  // with the table
+  if (tid == 0)
+    T.carrier = ~0u;
+  __syncthreads();
+  if (T.ok && b.chunk_bytes >= kTreelessMinChunk) {
+    const uint64_t seg_first = chunk * b.segs_per_chunk;
+    for (uint32_t bi = tid; bi < blocks_per_chunk; bi += blockDim.x) {
+      uint32_t nlit;
+      bool same;
+      block_literals(meta, seg_first, b.chunk_bytes, bi, nlit, same);
+      if (block_uses_table(true, nlit, same))
+        atomicMin(&T.carrier, bi);
+    }
   }
   __syncthreads();
   ChunkTable& ct = tables[chunk];
@@ -911,10 +1011,11 @@ zstd_table_k(const uint32_t* chunk_hist, ChunkTable* tables)
   if (tid == 0) {
     ct.desc_len = uint32_t(dl);
     ct.ok = T.ok;
+    ct.carrier = T.carrier;
   }
 }
 
-__global__ void __launch_bounds__(kBlockThreads, 4)
+__global__ void __launch_bounds__(kBlockThreads, 8)
 zstd_block_k(CodecBatch b,
              const __grid_constant__ PredefTables pre,
              const Seq* seqs,
@@ -1005,12 +1106,21 @@ zstd_block_k(CodecBatch b,
   __syncthreads();
   const uint32_t nlit = S.nlit, nseq = S.nseq;
   if (tid == 0) {
-    // literals section mode (the exact Huffman size decides below)
+    // literals section mode (the exact Huffman size decides below).  In a
+    // treeless chunk the carrier block describes the table and is always
+    // kept as a compressed block; later blocks refer to its description.
     S.lit_mode = 0;
+    S.with_desc = 1;
+    S.forced = 0;
     if (nlit > 0 && S.lit_same)
       S.lit_mode = 1;
-    else if (nlit >= 256 && ct.ok)
+    else if (block_uses_table(ct.ok, nlit, false)) {
       S.lit_mode = 2;
+      if (ct.carrier != ~0u) {
+        S.with_desc = bi == ct.carrier;
+        S.forced = bi == ct.carrier;
+      }
+    }
   }
   __syncthreads();
 
@@ -1076,7 +1186,7 @@ zstd_block_k(CodecBatch b,
         ssz[s] = S.stream_bits[s] / 8 + 1; // end mark + padding
         tot += ssz[s];
       }
-      const uint32_t dlen = ct.desc_len;
+      const uint32_t dlen = S.with_desc ? ct.desc_len : 0;
       const uint32_t csize = dlen + 6 + tot;
       const uint32_t big = max(nlit, csize);
       const uint32_t hdr = big < 1024 ? 3 : (big < 16384 ? 4 : 5);
@@ -1087,13 +1197,16 @@ zstd_block_k(CodecBatch b,
         S.stream_pos[s] = pos;
         pos += ssz[s];
       }
-      if (csize + hdr >= nlit + 3 || S.lit_missing) // not worth it / no code
+      // not worth it / a literal without a code (the carrier keeps its
+      // table: later blocks of the chunk depend on its description)
+      if (!S.forced && (csize + hdr >= nlit + 3 || S.lit_missing))
         S.lit_mode = 0;
       else {
         uint8_t* o = stage + 3;
         const uint32_t sf = hdr == 3 ? 1 : (hdr == 4 ? 2 : 3);
         const int nbits = hdr == 3 ? 10 : (hdr == 4 ? 14 : 18);
-        const uint64_t h = 2u | (sf << 2) | (uint64_t(nlit) << 4) |
+        const uint32_t type = S.with_desc ? 2u : 3u; // compressed / treeless
+        const uint64_t h = type | (sf << 2) | (uint64_t(nlit) << 4) |
                            (uint64_t(csize) << (4 + nbits));
         put_le(o, h, hdr);
         o += hdr + dlen; // the description is copied by all threads below
@@ -1106,7 +1219,7 @@ zstd_block_k(CodecBatch b,
     // packing ORs into it (16-byte stores between byte-wise ends)
     __syncthreads();
     if (S.lit_mode == 2) {
-      const uint32_t dlen = ct.desc_len;
+      const uint32_t dlen = S.with_desc ? ct.desc_len : 0;
       for (uint32_t i = tid; i < dlen; i += blockDim.x)
         stage[3 + S.lit_hdr + i] = ct.desc[i];
       const uint32_t z0 = S.stream_pos[0];
@@ -1329,14 +1442,16 @@ zstd_block_k(CodecBatch b,
     S.seq_csize = fits ? bs0 + nbytes - 3 : 0xFFFFFFFFu;
   __syncthreads();
   if (tid == 0) {
-    const uint32_t csize = min(S.seq_csize, bsize);
+    // a carrier stays compressed even when larger than its input (it
+    // always fits the staging, see kStageBytes)
+    const uint32_t csize = S.seq_csize; // ~0u: did not fit
     const bool last = b1 == b.chunk_bytes;
     uint32_t total;
     if (S.all_same) { // RLE block: one byte
       put_le(stage, (last ? 1u : 0u) | (1u << 1) | (bsize << 3), 3);
       stage[3] = in[b0];
       total = 4;
-    } else if (csize >= bsize) { // raw block
+    } else if (csize == 0xFFFFFFFFu || (!S.forced && csize >= bsize)) { // raw block
       put_le(stage, (last ? 1u : 0u) | (bsize << 3), 3);
       total = 3 + bsize;
       S.lit_mode = 3; // marks "copy input" for the threads below
@@ -1466,7 +1581,8 @@ cudaError_t launch_zstd(CodecBatch b, void* scratch, cudaStream_t st)
     fse_build(t.of, kOFNormH, 29, 5, spread, fill);
     return t;
   }();
-  CHUCKY_LAUNCH(zstd_table_k, unsigned(b.n_chunks), kBlockThreads, 0, st, hist, tables);
+  CHUCKY_LAUNCH(zstd_table_k, unsigned(b.n_chunks), kTableThreads, 0, st, b, hist, meta,
+                tables, bpc);
   if ((e = cudaGetLastError()) != cudaSuccess)
     return e;
   CHUCKY_LAUNCH(zstd_block_k, unsigned(blocks), kBlockThreads, kBlockBytes + 16, st, b,

@@ -191,6 +191,26 @@ inline unsigned atomicOr(unsigned* p, unsigned v)
     simt::fail("misaligned 32-bit atomicOr");
   return std::atomic_ref<unsigned>(*p).fetch_or(v);
 }
+inline unsigned long long atomicAdd(unsigned long long* p, unsigned long long v)
+{
+  return std::atomic_ref<unsigned long long>(*p).fetch_add(v);
+}
+inline unsigned atomicMin(unsigned* p, unsigned v)
+{
+  std::atomic_ref<unsigned> a(*p);
+  unsigned cur = a.load();
+  while (v < cur && !a.compare_exchange_weak(cur, v)) {
+  }
+  return cur;
+}
+inline unsigned atomicMax(unsigned* p, unsigned v)
+{
+  std::atomic_ref<unsigned> a(*p);
+  unsigned cur = a.load();
+  while (cur < v && !a.compare_exchange_weak(cur, v)) {
+  }
+  return cur;
+}
 inline int atomicMax(int* p, int v)
 {
   std::atomic_ref<int> a(*p);
