@@ -54,8 +54,13 @@ constexpr uint32_t kLaneExtend = 64;
 // positions probed per lane step grow by one for every 2^kSearchStrength
 // literals since the last match (sparse probing of incompressible runs)
 constexpr int kSearchStrength = CHUCKY_SEARCH_STRENGTH;
-// segments of the region before a warp's own that enter its table
+// segments of the region before a warp's own that enter its table, and the
+// stride of the positions entered
 constexpr uint32_t kHistorySegs = CHUCKY_HISTORY_SEGS;
+#ifndef CHUCKY_HISTORY_STRIDE
+#define CHUCKY_HISTORY_STRIDE 2
+#endif
+constexpr uint32_t kHistoryStride = CHUCKY_HISTORY_STRIDE;
 static_assert((2u << kHashLog) >= kSegBytes / 8,
               "a warp's table holds its literal bitmap");
 
@@ -139,8 +144,8 @@ __device__ inline SegInfo lz77_parse_segment(const uint32_t* words,
   // history: the region's positions before this segment
   const uint32_t hist0 =
     first > kHistorySegs * kSegBytes ? first - kHistorySegs * kSegBytes : 0;
-  for (uint32_t w0 = hist0; w0 < first; w0 += 32) {
-    const uint32_t q = w0 + lane;
+  for (uint32_t w0 = hist0; w0 < first; w0 += 32 * kHistoryStride) {
+    const uint32_t q = w0 + lane * kHistoryStride;
     const uint32_t h = hash4(word_at(words, q));
     __syncwarp();
     table[h] = uint16_t(q);
@@ -331,7 +336,26 @@ __device__ inline uint32_t lz77_compact_literals(uint32_t* words,
     ex -= cnt;
     __syncwarp();
     const uint32_t d = out + ex;
-    uint32_t mr = __funnelshift_r(m, m, rot); // m rotated right by rot
+    // all 32 bytes literal (the common case): whole aligned words, bytes
+    // only at the unaligned ends
+    uint32_t mr = m == 0xFFFFFFFFu ? 0u : __funnelshift_r(m, m, rot);
+    if (m == 0xFFFFFFFFu) {
+      const uint32_t w8[9] = { lo4.x, lo4.y, lo4.z, lo4.w, hi4.x, hi4.y, hi4.z, hi4.w, 0 };
+      const uint32_t h = (4 - (d & 3)) & 3; // head bytes
+#pragma unroll
+      for (uint32_t j = 0; j < 3; ++j)
+        if (j < h)
+          bytes[d + j] = uint8_t(w8[0] >> (8 * j));
+      uint32_t* dw = reinterpret_cast<uint32_t*>(bytes + d + h);
+#pragma unroll
+      for (int i = 0; i < 8; ++i)
+        if (i < 7 || h == 0)
+          dw[i] = __funnelshift_r(w8[i], w8[i + 1], h * 8);
+#pragma unroll
+      for (uint32_t j = 1; j < 4; ++j)
+        if (h > 0 && j >= h)
+          bytes[d + 28 + j] = uint8_t(w8[7] >> (8 * j));
+    }
     while (mr) {
       const int i = (__ffs(int(mr)) - 1 + rot) & 31;
       mr &= mr - 1;

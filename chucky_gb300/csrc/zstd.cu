@@ -201,26 +201,6 @@ zstd_find_k(CodecBatch b,
   if (has)
     info = lz77_parse_segment(words, r0, s0, s1, s1, s1, tables[w], out, kMinMatch);
   __syncthreads(); // the region is no longer needed as history
-  if (!has)
-    return;
-  uint32_t matched = 0;
-  for (uint32_t i = lane; i < info.nseq; i += 32)
-    matched += out[i].match;
-  for (int o = 16; o; o >>= 1)
-    matched += __shfl_xor_sync(0xffffffffu, matched, o);
-  // single-valued input?
-  const uint8_t* sb = reinterpret_cast<const uint8_t*>(words) + (s0 - r0);
-  const uint32_t n = s1 - s0;
-  const uint8_t in0 = sb[0];
-  const uint32_t pat = in0 * 0x01010101u;
-  const uint32_t* sw = words + (s0 - r0) / 4;
-  bool same = true;
-  for (uint32_t i = lane; i < n / 4; i += 32)
-    same &= sw[i] == pat;
-  for (uint32_t i = n / 4 * 4 + lane; i < n; i += 32)
-    same &= sb[i] == in0;
-  const bool in_same = __all_sync(0xffffffffu, same);
-  // literals: compacted in place, counted, copied out
   uint32_t* bitmap = reinterpret_cast<uint32_t*>(tables[w]);
   uint32_t* hist = bitmap + (kSegBytes / 32 + 31) / 32 * 32; // after the bitmap
   static_assert((kSegBytes / 32 + 31) / 32 * 32 + 256 <= (1u << kHashLog) / 2,
@@ -228,31 +208,57 @@ zstd_find_k(CodecBatch b,
   for (int i = lane; i < 256; i += 32)
     hist[i] = 0;
   __syncwarp();
-  const uint32_t nlit = lz77_compact_literals(words, r0, s0, s1, out, info.nseq, bitmap);
-  __syncwarp();
-  // count the literals (consecutive lanes, consecutive bytes: few lanes
-  // share a symbol within one step) and test whether they are one value
-  const uint8_t lit0 = nlit ? sb[0] : 0;
-  same = true;
-  for (uint32_t i = lane; i < nlit; i += 32) {
-    const uint8_t c = sb[i];
-    atomicAdd(hist + c, 1u);
-    same &= c == lit0;
+  if (has) {
+    uint32_t matched = 0;
+    for (uint32_t i = lane; i < info.nseq; i += 32)
+      matched += out[i].match;
+    for (int o = 16; o; o >>= 1)
+      matched += __shfl_xor_sync(0xffffffffu, matched, o);
+    // single-valued input?
+    const uint8_t* sb = reinterpret_cast<const uint8_t*>(words) + (s0 - r0);
+    const uint32_t n = s1 - s0;
+    const uint8_t in0 = sb[0];
+    const uint32_t pat = in0 * 0x01010101u;
+    const uint32_t* sw = words + (s0 - r0) / 4;
+    bool same = true;
+    for (uint32_t i = lane; i < n / 4; i += 32)
+      same &= sw[i] == pat;
+    for (uint32_t i = n / 4 * 4 + lane; i < n; i += 32)
+      same &= sb[i] == in0;
+    const bool in_same = __all_sync(0xffffffffu, same);
+    // literals: compacted in place, counted, copied out
+    const uint32_t nlit =
+      lz77_compact_literals(words, r0, s0, s1, out, info.nseq, bitmap);
+    __syncwarp();
+    // count the literals (consecutive lanes, consecutive bytes: few lanes
+    // share a symbol within one step) and test whether they are one value
+    const uint8_t lit0 = nlit ? sb[0] : 0;
+    same = true;
+    for (uint32_t i = lane; i < nlit; i += 32) {
+      const uint8_t c = sb[i];
+      atomicAdd(hist + c, 1u);
+      same &= c == lit0;
+    }
+    const bool lit_same = __all_sync(0xffffffffu, same);
+    const uint4* src = reinterpret_cast<const uint4*>(sb);
+    uint4* dst = reinterpret_cast<uint4*>(litbuf + seg * kSegBytes);
+    for (uint32_t i = lane; i < (nlit + 15) / 16; i += 32)
+      dst[i] = src[i];
+    if (lane == 0)
+      meta[seg] = ZSeg{ info.nseq, info.trailing, matched,
+                        uint32_t(lit0) | (lit_same ? 1u << 8 : 0u) |
+                          (uint32_t(in0) << 16) | (in_same ? 1u << 24 : 0u) };
   }
-  const bool lit_same = __all_sync(0xffffffffu, same);
-  const uint4* src = reinterpret_cast<const uint4*>(sb);
-  uint4* dst = reinterpret_cast<uint4*>(litbuf + seg * kSegBytes);
-  for (uint32_t i = lane; i < (nlit + 15) / 16; i += 32)
-    dst[i] = src[i];
-  __syncwarp();
+  // the CTA's literal histogram, added to its chunk's once
+  __syncthreads();
   uint32_t* ch = chunk_hist + chunk * 256;
-  for (int i = lane; i < 256; i += 32)
-    if (hist[i])
-      atomicAdd(ch + i, hist[i]);
-  if (lane == 0)
-    meta[seg] = ZSeg{ info.nseq, info.trailing, matched,
-                      uint32_t(lit0) | (lit_same ? 1u << 8 : 0u) |
-                        (uint32_t(in0) << 16) | (in_same ? 1u << 24 : 0u) };
+  for (int i = threadIdx.x; i < 256; i += blockDim.x) {
+    uint32_t t = 0;
+    for (int v = 0; v < int(kSegsPerRegion); ++v)
+      t += (reinterpret_cast<uint32_t*>(tables[v]) + (kSegBytes / 32 + 31) / 32 * 32)[i];
+    if (t)
+      atomicAdd(ch + i, t);
+  }
 }
 
 // ---------------------------------------------------------------------------
