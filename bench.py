@@ -53,11 +53,15 @@ def make_cubes(seed=7):
     return u16, f32
 
 
+EPOCHS_PER_BATCH = int(os.environ.get("CHUCKY_BENCH_EPOCHS_PER_BATCH", "4"))
+
+
 def make_config(dtype, reduce):
     dims = capi.make_dims([dict(size=SIDE, chunk=CHUNK, cps=4, downsample=1, name=n)
                            for n in "zyx"])
     cfg = capi.make_config(dims, dtype=dtype, codec="zstd", level=3, reduce=reduce,
-                           append_reduce="mean", max_nlod=4, epochs_per_batch=4,
+                           append_reduce="mean", max_nlod=4,
+                           epochs_per_batch=EPOCHS_PER_BATCH,
                            buffer_capacity_bytes=128 << 20)
     cfg._dims = dims
     return cfg

@@ -118,6 +118,31 @@ __device__ __forceinline__ void lz77_stage_region(const uint8_t* base,
   __syncthreads();
 }
 
+// Length of the match of position q against cand (< q), up to kLaneExtend
+// bytes, ending at or before `end` (one lane).
+__device__ __forceinline__ uint32_t lane_match(const uint32_t* words,
+                                               const uint8_t* bytes,
+                                               uint32_t q,
+                                               uint32_t cand,
+                                               uint32_t end)
+{
+  uint32_t len = 4;
+  while (len < kLaneExtend) {
+    if (q + len + 4 > end) { // the last bytes before `end`, one by one
+      while (q + len < end && bytes[q + len] == bytes[cand + len])
+        ++len;
+      break;
+    }
+    const uint32_t x = word_at(words, q + len) ^ word_at(words, cand + len);
+    if (x) {
+      len += uint32_t(__ffs(int(x)) - 1) >> 3;
+      break;
+    }
+    len += 4;
+  }
+  return len;
+}
+
 // Parse segment [s0, s1) of a chunk whose bytes from r0 (the region start,
 // r0 <= s0) on are staged in `words`.  Matches may start at positions in
 // [s0, start_limit), reach back to r0 and end at or before `match_end`.
@@ -152,76 +177,18 @@ __device__ inline SegInfo lz77_parse_segment(const uint32_t* words,
   }
   __syncwarp();
   uint32_t w0 = first, p = first, lit_start = first, nseq = 0;
-  while (w0 < lim) {
-    const uint32_t step = 1 + ((w0 > lit_start ? w0 - lit_start : 0) >> kSearchStrength);
-    const uint32_t q = w0 + lane * step;
-    const bool valid = q < lim && q + 4 <= end;
-    uint32_t v = 0, h = 0, cand = 0;
-    bool ok = false;
-    if (valid) {
-      v = word_at(words, q);
-      h = hash4(v);
-      const uint16_t t = table[h];
-      // entries can be ahead of q: a window skipped into a long match
-      // leaves later positions in the table
-      if (t != 0xFFFF && t < q) {
-        cand = t;
-        ok = word_at(words, cand) == v;
-      }
-    }
-    // runs and short periods (1, 2, 4 bytes) match positions of this same
-    // window that are not in the table yet
-    {
-      const uint32_t v1 = __shfl_up_sync(0xffffffffu, v, 1);
-      const uint32_t v2 = __shfl_up_sync(0xffffffffu, v, 2);
-      const uint32_t v4 = __shfl_up_sync(0xffffffffu, v, 4);
-      if (valid && !ok) {
-        if (lane >= 1 && v1 == v) {
-          cand = q - step;
-          ok = true;
-        } else if (lane >= 2 && v2 == v) {
-          cand = q - 2 * step;
-          ok = true;
-        } else if (lane >= 4 && v4 == v) {
-          cand = q - 4 * step;
-          ok = true;
-        }
-      }
-    }
-    // this lane's match length, up to kLaneExtend bytes
-    uint32_t len = 0;
-    if (ok) {
-      len = 4;
-      while (len < kLaneExtend) {
-        if (q + len + 4 > end) { // the last bytes before `end`, one by one
-          while (q + len < end && bytes[q + len] == bytes[cand + len])
-            ++len;
-          break;
-        }
-        const uint32_t x = word_at(words, q + len) ^ word_at(words, cand + len);
-        if (x) {
-          len += uint32_t(__ffs(int(x)) - 1) >> 3;
-          break;
-        }
-        len += 4;
-      }
-    }
-    __syncwarp();
-    if (valid)
-      table[h] = uint16_t(q);
-    __syncwarp();
-    unsigned hits = __ballot_sync(0xffffffffu, ok && len >= min_match);
-    // greedy parse through this window
+  // greedy parse of one window's hits (lanes at or after the parse point)
+  auto take = [&](unsigned hits, uint32_t base, uint32_t step, uint32_t cand,
+                  uint32_t len) {
     for (;;) {
-      // first lane at or after the parse point
-      const uint32_t from = p > w0 ? (p - w0 + step - 1) / step : 0;
+      const uint32_t from = p > base ? (p - base + step - 1) / step : 0;
       if (from >= 32)
         break;
       const unsigned m = hits & (0xffffffffu << from);
       if (!m)
         break;
       const int k = __ffs(int(m)) - 1;
-      const uint32_t mpos = w0 + k * step;
+      const uint32_t mpos = base + k * step;
       const uint32_t src = __shfl_sync(0xffffffffu, cand, k);
       uint32_t mlen = __shfl_sync(0xffffffffu, len, k);
       if (mlen >= kLaneExtend) { // long match: the warp extends it
@@ -243,8 +210,69 @@ __device__ inline SegInfo lz77_parse_segment(const uint32_t* words,
       p = mpos + mlen;
       lit_start = p;
     }
-    // next window; skip windows that lie inside a long match
-    w0 = p >= w0 + 64 * step ? p : w0 + 32 * step;
+  };
+  // Two windows (a, b) per iteration, probed side by side: b's probes do
+  // not see a's positions in the table (b finds them only as runs or short
+  // periods), in exchange for twice the independent work per step.
+  while (w0 < lim) {
+    const uint32_t step = 1 + ((w0 > lit_start ? w0 - lit_start : 0) >> kSearchStrength);
+    const uint32_t qa = w0 + lane * step, qb = qa + 32 * step;
+    const bool va = qa < lim && qa + 4 <= end, vb = qb < lim && qb + 4 <= end;
+    uint32_t xa = 0, xb = 0, ha = 0, hb = 0, ca = 0, cb = 0;
+    bool oka = false, okb = false;
+    if (va) {
+      xa = word_at(words, qa);
+      ha = hash4(xa);
+    }
+    if (vb) {
+      xb = word_at(words, qb);
+      hb = hash4(xb);
+    }
+    const uint16_t ta = va ? table[ha] : uint16_t(0xFFFF);
+    const uint16_t tb = vb ? table[hb] : uint16_t(0xFFFF);
+    // entries can be ahead of q: a window skipped into a long match leaves
+    // later positions in the table
+    if (ta != 0xFFFF && ta < qa) {
+      ca = ta;
+      oka = word_at(words, ca) == xa;
+    }
+    if (tb != 0xFFFF && tb < qb) {
+      cb = tb;
+      okb = word_at(words, cb) == xb;
+    }
+    // runs and short periods (1, 2, 4 positions back) within the windows
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      const uint32_t d = 1u << i;
+      const uint32_t pa = __shfl_up_sync(0xffffffffu, xa, d);
+      const uint32_t pb0 = __shfl_up_sync(0xffffffffu, xb, d);
+      const uint32_t pb1 = __shfl_sync(0xffffffffu, xa, (lane + 32 - d) & 31);
+      const uint32_t pb = uint32_t(lane) >= d ? pb0 : pb1;
+      if (va && !oka && uint32_t(lane) >= d && pa == xa) {
+        ca = qa - d * step;
+        oka = true;
+      }
+      // (when b's position is valid every earlier position is too)
+      if (vb && !okb && pb == xb) {
+        cb = qb - d * step;
+        okb = true;
+      }
+    }
+    const uint32_t la = oka ? lane_match(words, bytes, qa, ca, end) : 0;
+    const uint32_t lb = okb ? lane_match(words, bytes, qb, cb, end) : 0;
+    __syncwarp();
+    if (va)
+      table[ha] = uint16_t(qa);
+    __syncwarp();
+    if (vb)
+      table[hb] = uint16_t(qb);
+    __syncwarp();
+    const unsigned hits_a = __ballot_sync(0xffffffffu, oka && la >= min_match);
+    const unsigned hits_b = __ballot_sync(0xffffffffu, okb && lb >= min_match);
+    take(hits_a, w0, step, ca, la);
+    take(hits_b, w0 + 32 * step, step, cb, lb);
+    // next windows; skip those inside a long match
+    w0 = p >= w0 + 128 * step ? p : w0 + 64 * step;
   }
   __syncwarp();
   return SegInfo{ nseq, (s1 - r0) - lit_start };
