@@ -93,6 +93,38 @@ lod_tile_k(LodTileArgs a)
     ext[k] = uint32_t(rem < uint64_t(TE) ? rem : uint64_t(TE));
   }
   const uint64_t fixed0 = a.lv[0].chunk_fixed ? a.lv[0].chunk_fixed[b] : 0;
+  // Fast path (2-D, whole tile inside one chunk, rows contiguous in the
+  // input and in the chunk, 16-byte aligned): rows move as 16-byte vectors.
+  bool fast = D == 2 && sizeof(T) <= 16;
+  uint64_t in0 = 0, out0 = fixed0;
+#pragma unroll
+  for (int k = 0; k < D; ++k) {
+    fast &= ext[k] == uint32_t(TE) && a.cs[k] % TE == 0;
+    in0 += uint64_t(org[k]) * a.in_stride[k];
+    out0 += uint64_t(org[k] / a.cs[k]) * a.lv[0].S[k] +
+            uint64_t(org[k] % a.cs[k]) * a.lv[0].s[k];
+  }
+  if (D == 2) {
+    constexpr uint64_t kVecElems = 16 / sizeof(T);
+    fast &= a.in_stride[D - 1] == 1 && a.lv[0].s[D - 1] == 1 &&
+            (a.gather_fixed[b] + in0) % kVecElems == 0 &&
+            uint64_t(a.in_stride[0]) % kVecElems == 0 && out0 % kVecElems == 0 &&
+            a.lv[0].s[0] % kVecElems == 0 &&
+            (reinterpret_cast<uintptr_t>(lin) & 15) == 0 &&
+            (reinterpret_cast<uintptr_t>(slot) & 15) == 0;
+  }
+  if (fast) {
+    constexpr int kVec = 16 / int(sizeof(T) > 16 ? 16 : sizeof(T)); // elements per vector
+    constexpr int kVpr = TE / kVec;                                  // vectors per row
+    for (int i = threadIdx.x; i < TE * kVpr; i += kTileThreads) {
+      const int row = i / kVpr, col = i % kVpr;
+      const uint4 v = *reinterpret_cast<const uint4*>(
+        lin + in0 + uint64_t(row) * a.in_stride[0] + uint64_t(col) * kVec);
+      *reinterpret_cast<uint4*>(cur + row * TE + col * kVec) = v;
+      *reinterpret_cast<uint4*>(slot + out0 + uint64_t(row) * a.lv[0].s[0] +
+                                uint64_t(col) * kVec) = v;
+    }
+  } else
   for (int i = threadIdx.x; i < TN; i += kTileThreads) {
     uint32_t x[3], in = 1;
     int r = i;
@@ -115,9 +147,10 @@ lod_tile_k(LodTileArgs a)
   __syncthreads();
 
   // ---- levels 1.. ----
-  int edge = TE;
+  int edge = TE, elog = TL;
   for (int l = 1; l < a.nlod && l <= TL; ++l) {
     const int pe = edge >> 1; // parent tile edge
+    const int plog = elog - 1;
     int pn = 1;
 #pragma unroll
     for (int k = 0; k < D; ++k)
@@ -134,15 +167,25 @@ lod_tile_k(LodTileArgs a)
     const bool fold = (a.fold_mask >> l) & 1;
     const bool emit = (a.emit_mask >> l) & 1;
     const uint64_t fixedl = a.lv[l].chunk_fixed ? a.lv[l].chunk_fixed[b] : 0;
+    // the parent tile lies inside one chunk along every dim: chunk offsets
+    // are a tile base plus within-chunk strides (no per-element division)
+    bool inchunk = true;
+    uint64_t tbase = fixedl;
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+      inchunk &= a.cs[k] % uint32_t(pe) == 0;
+      tbase += uint64_t(porg[k] / a.cs[k]) * a.lv[l].S[k] +
+               uint64_t(porg[k] % a.cs[k]) * a.lv[l].s[k];
+    }
     for (int i = threadIdx.x; i < pn; i += kTileThreads) {
       uint32_t p[3], in = 1;
       int r = i;
 #pragma unroll
       for (int k = D - 1; k >= 0; --k) {
-        const int lp = r % pe;
+        const int lp = r & (pe - 1);
         p[k] = uint32_t(lp);
         in &= uint32_t(lp) < pext[k];
-        r /= pe;
+        r >>= plog;
       }
       if (!in)
         continue;
@@ -157,7 +200,7 @@ lod_tile_k(LodTileArgs a)
         for (int k = 0; k < D; ++k) {
           const uint32_t c = 2 * p[k] + ((z >> k) & 1);
           ok &= c < cext[k];
-          ci = ci * edge + int(c);
+          ci = (ci << elog) + int(c);
         }
         if (ok)
           win[n++] = cur[ci];
@@ -166,12 +209,17 @@ lod_tile_k(LodTileArgs a)
       int pi = 0;
 #pragma unroll
       for (int k = 0; k < D; ++k)
-        pi = pi * pe + int(p[k]);
+        pi = (pi << plog) + int(p[k]);
       nxt[pi] = v;
       uint32_t gx[3];
+      uint64_t pos = tbase;
 #pragma unroll
-      for (int k = 0; k < D; ++k)
+      for (int k = 0; k < D; ++k) {
         gx[k] = porg[k] + p[k];
+        pos += uint64_t(p[k]) * a.lv[l].s[k];
+      }
+      if (!inchunk)
+        pos = fixedl + chunk_pos<D>(a, l, gx);
       if (fold) {
         // dense accumulator [fixed][row-major level coords]
         uint64_t ai = 0;
@@ -184,10 +232,9 @@ lod_tile_k(LodTileArgs a)
         const T av = cnt == 0 ? v : fold_one<T>(*acc, v, l, a.append_method);
         *acc = av;
         if (emit)
-          slot[fixedl + chunk_pos<D>(a, l, gx)] =
-            emit_one<T>(av, cnt + 1, a.append_method);
+          slot[pos] = emit_one<T>(av, cnt + 1, a.append_method);
       } else if (emit) {
-        slot[fixedl + chunk_pos<D>(a, l, gx)] = v;
+        slot[pos] = v;
       }
     }
     __syncthreads();
@@ -201,6 +248,7 @@ lod_tile_k(LodTileArgs a)
       ext[k] = pext[k];
     }
     edge = pe;
+    elog = plog;
     __syncthreads();
   }
 }

@@ -60,6 +60,14 @@ CASES = [
      dict(reduce="mean", append_reduce="max"), 5),
     ("aligned_shards", [D(size=8, chunk=2, cps=2), D(size=16, chunk=8, cps=1),
                         D(size=16, chunk=8, cps=2)], dict(shard_alignment=512), 4),
+    # 64x64 LOD tiles inside 64-wide chunks (vector path) next to ragged
+    # edge tiles (element path)
+    ("lod2d_tiles", [D(size=0, chunk=2, cps=1), D(size=200, chunk=64, cps=2, downsample=1),
+                     D(size=320, chunk=64, cps=2, downsample=1)], dict(reduce="mean"), 3),
+    ("lod2d_dim0_tiles", [D(size=0, chunk=4, cps=1, downsample=1),
+                          D(size=128, chunk=128, cps=1, downsample=1),
+                          D(size=192, chunk=64, cps=2, downsample=1)],
+     dict(reduce="max", append_reduce="mean"), 5),
 ]
 
 DTYPES_ALL = ["u8", "u16", "u32", "u64", "i8", "i16", "i32", "i64", "f32", "f64"]
