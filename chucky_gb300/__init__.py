@@ -28,6 +28,8 @@ EXPORTS = [
     "dims_set_chunk_sizes", "dims_budget_chunk_size", "dims_set_shard_counts",
     "dims_budget_chunk_bytes", "dims_n_append", "dims_validate", "dims_print",
     "codec_is_blosc", "codec_is_gpu_supported",
+    "multiarray_tile_stream_gpu_create", "multiarray_tile_stream_gpu_destroy",
+    "multiarray_tile_stream_gpu_writer", "multiarray_tile_stream_gpu_get_metrics",
 ]
 
 

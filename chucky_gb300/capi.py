@@ -115,6 +115,19 @@ Writer._fields_ = [
     ("flush", C.CFUNCTYPE(WriterResult, C.POINTER(Writer)))]
 
 
+# include/multiarray.gpu.h (src/multiarray.cpu.h:6-26)
+MULTIARRAY_OK, MULTIARRAY_FAIL, MULTIARRAY_FINISHED, MULTIARRAY_NOT_FLUSHABLE = range(4)
+
+
+class MultiarrayWriter(C.Structure):
+    pass
+
+
+MultiarrayWriter._fields_ = [
+    ("update", C.CFUNCTYPE(WriterResult, C.POINTER(MultiarrayWriter), C.c_int, Slice)),
+    ("flush", C.CFUNCTYPE(WriterResult, C.POINTER(MultiarrayWriter)))]
+
+
 class IoEvent(C.Structure):
     _fields_ = [("seq", C.c_uint64)]
 
