@@ -46,7 +46,7 @@ constexpr uint32_t kRegionStageWords = kRegionBytes / 4 + 4;
 // bytes a lane measures of its own match before the warp takes over
 constexpr uint32_t kLaneExtend = 64;
 #ifndef CHUCKY_SEARCH_STRENGTH
-#define CHUCKY_SEARCH_STRENGTH 8
+#define CHUCKY_SEARCH_STRENGTH 6
 #endif
 #ifndef CHUCKY_HISTORY_SEGS
 #define CHUCKY_HISTORY_SEGS 1

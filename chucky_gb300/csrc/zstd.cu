@@ -1306,8 +1306,6 @@ zstd_block_k(CodecBatch b,
       if (fill > 0)
         atomicOr(wbase + word, uint32_t(acc));
     }
-  } else if (tid == 0 && nlit > 0 && S.lit_mode == 0) {
-    // nothing to lay out yet (raw literals below)
   }
   __syncthreads();
 
