@@ -55,6 +55,10 @@ constexpr uint32_t kHufMaxBits = 11;
 // matches shorter than this cost more as a sequence than as literals
 constexpr uint32_t kMinMatch = CHUCKY_ZSTD_MIN_MATCH;
 
+// Per chunk: 256 literal counts of a 1-in-4 sample of the literal bytes,
+// then a 256-bit map of every literal byte value present.
+constexpr uint32_t kHistWords = 256 + 8;
+
 struct ZSeg
 {
   uint32_t nseq, trailing, matched; // matched = bytes covered by matches
@@ -174,7 +178,7 @@ __constant__ uint8_t kMLBits[53] = { 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0,
 // One CTA per region, a warp per segment.  Besides the sequences, every
 // segment leaves its literal bytes, compacted, in its slot of `litbuf`
 // (kSegBytes each), adds them to its chunk's literal histogram
-// (`chunk_hist`, 256 counts per chunk, zeroed before the launch) and
+// (`chunk_hist`, kHistWords per chunk, zeroed before the launch) and
 // records whether its input and its literals are single-valued.
 __global__ void __launch_bounds__(32 * kSegsPerRegion)
 zstd_find_k(CodecBatch b,
@@ -203,9 +207,10 @@ zstd_find_k(CodecBatch b,
   __syncthreads(); // the region is no longer needed as history
   uint32_t* bitmap = reinterpret_cast<uint32_t*>(tables[w]);
   uint32_t* hist = bitmap + (kSegBytes / 32 + 31) / 32 * 32; // after the bitmap
-  static_assert((kSegBytes / 32 + 31) / 32 * 32 + 256 <= (1u << kHashLog) / 2,
-                "bitmap and histogram fit in a warp's table");
-  for (int i = lane; i < 256; i += 32)
+  uint32_t* pres = hist + 256;
+  static_assert((kSegBytes / 32 + 31) / 32 * 32 + 256 + 8 <= (1u << kHashLog) / 2,
+                "bitmap, histogram and presence map fit in a warp's table");
+  for (int i = lane; i < 256 + 8; i += 32)
     hist[i] = 0;
   __syncwarp();
   if (has) {
@@ -230,14 +235,31 @@ zstd_find_k(CodecBatch b,
     const uint32_t nlit =
       lz77_compact_literals(words, r0, s0, s1, out, info.nseq, bitmap);
     __syncwarp();
-    // count the literals (consecutive lanes, consecutive bytes: few lanes
-    // share a symbol within one step) and test whether they are one value
+    // literal statistics, a word (4 bytes) per lane and step: every value
+    // present marks the presence map (one atomic the first time it is seen
+    // by this warp), one byte per word, rotating through the four byte
+    // positions, is counted; and whether the literals are all one value
     const uint8_t lit0 = nlit ? sb[0] : 0;
+    const uint32_t pat0 = lit0 * 0x01010101u;
     same = true;
-    for (uint32_t i = lane; i < nlit; i += 32) {
-      const uint8_t c = sb[i];
-      atomicAdd(hist + c, 1u);
-      same &= c == lit0;
+    const uint32_t* lw = reinterpret_cast<const uint32_t*>(sb);
+    for (uint32_t i = lane; i < (nlit + 3) / 4; i += 32) {
+      const uint32_t v = lw[i];
+      const uint32_t nb = min(4u, nlit - 4 * i); // bytes of this word in use
+      const uint32_t keep = nb == 4 ? 0xFFFFFFFFu : (1u << (8 * nb)) - 1;
+      same &= ((v ^ pat0) & keep) == 0;
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        if (uint32_t(k) < nb) {
+          const uint32_t c = (v >> (8 * k)) & 255;
+          const uint32_t bit = 1u << (c & 31);
+          if (!(pres[c >> 5] & bit))
+            atomicOr(pres + (c >> 5), bit);
+        }
+      }
+      const uint32_t k = i & 3;
+      if (k < nb)
+        atomicAdd(hist + ((v >> (8 * k)) & 255), 1u);
     }
     const bool lit_same = __all_sync(0xffffffffu, same);
     const uint4* src = reinterpret_cast<const uint4*>(sb);
@@ -249,15 +271,22 @@ zstd_find_k(CodecBatch b,
                         uint32_t(lit0) | (lit_same ? 1u << 8 : 0u) |
                           (uint32_t(in0) << 16) | (in_same ? 1u << 24 : 0u) };
   }
-  // the CTA's literal histogram, added to its chunk's once
+  // the CTA's literal statistics, added to its chunk's once
   __syncthreads();
-  uint32_t* ch = chunk_hist + chunk * 256;
-  for (int i = threadIdx.x; i < 256; i += blockDim.x) {
+  uint32_t* ch = chunk_hist + chunk * kHistWords;
+  for (int i = threadIdx.x; i < int(kHistWords); i += blockDim.x) {
     uint32_t t = 0;
-    for (int v = 0; v < int(kSegsPerRegion); ++v)
-      t += (reinterpret_cast<uint32_t*>(tables[v]) + (kSegBytes / 32 + 31) / 32 * 32)[i];
-    if (t)
-      atomicAdd(ch + i, t);
+    for (int v = 0; v < int(kSegsPerRegion); ++v) {
+      const uint32_t x =
+        (reinterpret_cast<uint32_t*>(tables[v]) + (kSegBytes / 32 + 31) / 32 * 32)[i];
+      t = i < 256 ? t + x : t | x;
+    }
+    if (t) {
+      if (i < 256)
+        atomicAdd(ch + i, t);
+      else
+        atomicOr(ch + i, t);
+    }
   }
 }
 
@@ -801,7 +830,9 @@ zstd_table_k(CodecBatch b,
   HuffScratch& x = T.hx;
   Huff& h = T.huff;
   if (tid < 256) {
-    T.hist[tid] = chunk_hist[chunk * 256 + tid];
+    // four times the sampled count, and at least 1 for every value present
+    const uint32_t* ch = chunk_hist + chunk * kHistWords;
+    T.hist[tid] = 4 * ch[tid] + ((ch[256 + (tid >> 5)] >> (tid & 31)) & 1);
     h.len[tid] = 0;
   }
   if (tid < 16)
@@ -1538,7 +1569,7 @@ size_t zstd_scratch_bytes(uint64_t n_chunks, uint32_t chunk_bytes)
     n_chunks * ((chunk_bytes + kBlockBytes - 1) / kBlockBytes);
   return segs * (kMaxSeqPerSeg * sizeof(Seq) + sizeof(ZSeg) + kSegBytes) +
          blocks * (kStageBytes + sizeof(uint32_t)) +
-         n_chunks * (256 * sizeof(uint32_t) + sizeof(ChunkTable)) + 2048;
+         n_chunks * (kHistWords * sizeof(uint32_t) + sizeof(ChunkTable)) + 2048;
 }
 
 cudaError_t launch_zstd(CodecBatch b, void* scratch, cudaStream_t st)
@@ -1561,14 +1592,14 @@ cudaError_t launch_zstd(CodecBatch b, void* scratch, cudaStream_t st)
   p += blocks * sizeof(uint32_t);
   p = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(p) + 255) & ~uintptr_t(255));
   uint32_t* hist = reinterpret_cast<uint32_t*>(p);
-  p += b.n_chunks * 256 * sizeof(uint32_t);
+  p += b.n_chunks * kHistWords * sizeof(uint32_t);
   ChunkTable* tables = reinterpret_cast<ChunkTable*>(p);
   p += b.n_chunks * sizeof(ChunkTable);
   p = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(p) + 255) & ~uintptr_t(255));
   uint8_t* litbuf = p; // segs * kSegBytes, read up to 20 bytes past a slot
   const uint32_t rpc = (b.chunk_bytes + kRegionBytes - 1) / kRegionBytes;
   cudaError_t e;
-  if ((e = cudaMemsetAsync(hist, 0, b.n_chunks * 256 * sizeof(uint32_t), st)) !=
+  if ((e = cudaMemsetAsync(hist, 0, b.n_chunks * kHistWords * sizeof(uint32_t), st)) !=
       cudaSuccess)
     return e;
   note_launches(4);
