@@ -53,7 +53,10 @@ def make_cubes(seed=7):
     return u16, f32
 
 
-EPOCHS_PER_BATCH = int(os.environ.get("CHUCKY_BENCH_EPOCHS_PER_BATCH", "4"))
+# two batches of two 64-slice epochs per array and step: the encoders of
+# the first batch overlap the LOD of the second, its copy to the host the
+# second's encoders
+EPOCHS_PER_BATCH = int(os.environ.get("CHUCKY_BENCH_EPOCHS_PER_BATCH", "2"))
 
 
 def make_config(dtype, reduce):
@@ -68,8 +71,8 @@ def make_config(dtype, reduce):
 
 
 WORKLOAD = ("256^3 u16 (mean LOD) + 256^3 f32 (median LOD), chunk 64^3, shard "
-            "4^3 chunks, 2x2x2 pyramid (3 levels), zstd-3, K=4 epochs per batch "
-            "(one batch per array), discard sink")
+            "4^3 chunks, 2x2x2 pyramid (3 levels), zstd-3, K=%d epochs per batch "
+            "(%d batches per array), discard sink" % (EPOCHS_PER_BATCH, 4 // EPOCHS_PER_BATCH))
 
 
 class Clocks:

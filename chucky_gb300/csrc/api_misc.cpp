@@ -355,7 +355,9 @@ tile_stream_gpu_memory_estimate(const tile_stream_configuration* config,
     return 1;
   const uint64_t K = P.K;
   info->staging_bytes = 2 * (P.epoch_bytes + 512);
-  info->chunk_pool_bytes = K * P.slot_bytes;
+  // two halves with a codec (LOD fills one while the encoders read the other)
+  info->chunk_pool_bytes =
+    K * P.slot_bytes * (config->codec.id == CODEC_NONE ? 1 : 2);
   const uint64_t nchunks = K * P.total_chunks;
   info->compressed_pool_bytes =
     config->codec.id == CODEC_NONE ? 0
@@ -371,6 +373,8 @@ tile_stream_gpu_memory_estimate(const tile_stream_configuration* config,
     agg_host += 2 * ((pos + 1) * 8 + pos * 8 + 8 + cap * M * P.max_out +
                      (sa ? (nsh + 1) * sa : 0) + 64);
     agg_dev += 4 * cap * M * 4 + (pos + 1) * 8;
+    if (config->codec.id != CODEC_NONE) // device copy of both delivery slots
+      agg_dev += 2 * (cap * M * P.max_out + (sa ? (nsh + 1) * sa : 0) + 64);
     shard += V.shard_inner_count * V.cps_total * 16;
   }
   info->aggregate_bytes = agg_dev;

@@ -34,10 +34,12 @@ int Stream::codec_init()
   return cudaMalloc(&codec_state, bytes) == cudaSuccess ? 0 : 1;
 }
 
-int Stream::codec_compress(uint64_t nchunks,
+int Stream::codec_compress(const uint8_t* pool,
+                           uint64_t nchunks,
                            const uint32_t* d_ids,
                            uint8_t* out,
-                           uint64_t* sizes)
+                           uint64_t* sizes,
+                           cudaStream_t st)
 {
   cudaError_t e = cudaSuccess;
   for (uint64_t first = 0; first < nchunks && e == cudaSuccess;
@@ -50,17 +52,17 @@ int Stream::codec_compress(uint64_t nchunks,
     b.out_stride = comp_stride;
     b.level = cfg.codec.level;
     if (d_ids) { // chunk slots listed explicitly
-      b.in = d_pool;
+      b.in = pool;
       b.out = out;
       b.out_sizes = sizes;
       b.chunk_ids = d_ids + first;
     } else { // slots first .. first + n - 1
-      b.in = d_pool + first * b.in_stride;
+      b.in = pool + first * b.in_stride;
       b.out = out + first * comp_stride;
       b.out_sizes = sizes + first;
     }
-    e = cfg.codec.id == CODEC_ZSTD ? launch_zstd(b, codec_state, s_comp)
-                                   : launch_lz4(b, codec_state, s_comp);
+    e = cfg.codec.id == CODEC_ZSTD ? launch_zstd(b, codec_state, st)
+                                   : launch_lz4(b, codec_state, st);
   }
   if (e != cudaSuccess) {
     std::fprintf(stderr, "chucky_gb300: %s encoder launch failed: %s\n",

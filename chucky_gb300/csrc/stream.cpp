@@ -127,6 +127,8 @@ int Stream::init(const tile_stream_configuration* c, shard_sink* sk)
   CK(cudaStreamCreateWithFlags(&s_copy, cudaStreamNonBlocking));
   CK(cudaStreamCreateWithFlags(&s_comp, cudaStreamNonBlocking));
   CK(cudaStreamCreateWithFlags(&s_agg, cudaStreamNonBlocking));
+  CK(cudaStreamCreateWithFlags(&s_enc, cudaStreamNonBlocking));
+  CK(cudaEventCreateWithFlags(&ev_pool_ready, cudaEventDisableTiming));
   for (auto& t : timers) {
     CK(cudaEventCreate(&t.a));
     CK(cudaEventCreate(&t.b));
@@ -138,10 +140,13 @@ int Stream::init(const tile_stream_configuration* c, shard_sink* sk)
     CK(cudaEventCreateWithFlags(&ev_codec_done[i], cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&ev_agg_done[i], cudaEventDisableTiming));
     CK(cudaEventRecord(ev_agg_done[i], s_comp));
+    CK(cudaEventRecord(ev_codec_done[i], s_enc));
     CK(cudaMalloc(&d_epoch[i], round_up(P.epoch_bytes, 256) + 256));
     CK(cudaEventRecord(ev_input_free[i], s_comp));
   }
-  const uint64_t pool_bytes = uint64_t(P.K) * P.slot_bytes;
+  const uint64_t half = uint64_t(P.K) * P.slot_bytes;
+  pool_half_bytes = cfg.codec.id == CODEC_NONE ? 0 : half;
+  const uint64_t pool_bytes = half + pool_half_bytes;
   CK(cudaMalloc(&d_pool, pool_bytes + 256)); // encoders read 8 B past a chunk
   CK(cudaMemsetAsync(d_pool, 0, pool_bytes, s_comp));
   const uint64_t nchunks = uint64_t(P.K) * P.total_chunks;
@@ -423,6 +428,10 @@ int Stream::setup_aggregate()
       CK(cudaHostAlloc(&D.offsets, (positions + 1) * 8, cudaHostAllocMapped));
       CK(cudaHostAlloc(&D.real_sizes, positions * 8 + 8, cudaHostAllocMapped));
       CK(cudaHostAlloc(&D.data, data, cudaHostAllocMapped));
+      // compressed batches are gathered in device memory and copied to the
+      // host by the copy engine (faster than SM stores over the link)
+      if (cfg.codec.id != CODEC_NONE)
+        CK(cudaMalloc(&D.d_data, data));
     }
     // shard state (src/zarr/shard_delivery.c:10-34)
     Shards& S = shards[l];
@@ -439,6 +448,8 @@ void Stream::release()
 {
   if (s_comp)
     cudaStreamSynchronize(s_comp);
+  if (s_enc)
+    cudaStreamSynchronize(s_enc);
   if (s_agg)
     cudaStreamSynchronize(s_agg);
   if (s_copy)
@@ -456,6 +467,7 @@ void Stream::release()
       cudaFreeHost(slot[i].lv[l].offsets);
       cudaFreeHost(slot[i].lv[l].real_sizes);
       cudaFreeHost(slot[i].lv[l].data);
+      cudaFree(slot[i].lv[l].d_data);
     }
   }
   for (auto& t : timers) {
@@ -474,6 +486,10 @@ void Stream::release()
   }
   if (s_agg)
     cudaStreamDestroy(s_agg);
+  if (s_enc)
+    cudaStreamDestroy(s_enc);
+  if (ev_pool_ready)
+    cudaEventDestroy(ev_pool_ready);
   if (d_sizes[1] != d_sizes[0])
     cudaFree(d_sizes[1]);
   cudaFree(d_sizes[0]);
@@ -508,7 +524,18 @@ void Stream::release()
 
 uint8_t* Stream::pool_slot(uint32_t e) const
 {
-  return d_pool + uint64_t(e) * P.slot_bytes;
+  return d_pool + next_slot * pool_half_bytes + uint64_t(e) * P.slot_bytes;
+}
+
+// Before the first write of a batch into its pool half: the encoders of the
+// batch that last used that half must be done reading it.
+int Stream::claim_pool()
+{
+  if (pool_half_bytes && !pool_claimed) {
+    CK(cudaStreamWaitEvent(s_comp, ev_codec_done[next_slot], 0));
+    pool_claimed = true;
+  }
+  return 0;
 }
 
 int Stream::run_epoch(uint64_t present)
@@ -519,6 +546,8 @@ int Stream::run_epoch(uint64_t present)
   if (present < layout.epoch_elements) // partial final epoch: fill value 0
     CK(cudaMemsetAsync(d_epoch[b] + present * P.bpe, 0,
                        (layout.epoch_elements - present) * P.bpe, s_comp));
+  if (claim_pool())
+    return 1;
   uint8_t* slot_ptr = pool_slot(accumulated);
   uint32_t mask = 1;
   if (!P.multiscale) {
@@ -619,8 +648,14 @@ int Stream::kick_batch(uint32_t n_epochs, const uint32_t* epoch_masks)
   if (S.busy && deliver(si)) // cannot happen with drain-before-kick
     return 1;
   const uint64_t nchunks = uint64_t(n_epochs) * P.total_chunks;
-  const uint8_t* comp = d_pool;
-  if (cfg.codec.id != CODEC_NONE) {
+  const uint8_t* comp = d_pool + si * pool_half_bytes;
+  const bool coded = cfg.codec.id != CODEC_NONE;
+  // the aggregation's LUT uploads ride on the stream that precedes it
+  const cudaStream_t su = coded ? s_enc : s_comp;
+  if (coded) {
+    // the encoders start once this batch's pool half is filled
+    CK(cudaEventRecord(ev_pool_ready, s_comp));
+    CK(cudaStreamWaitEvent(s_enc, ev_pool_ready, 0));
     // encode only the chunks of active (epoch, level) pairs
     uint32_t* ids = h_chunk_ids[si];
     uint64_t n = 0;
@@ -634,17 +669,17 @@ int Stream::kick_batch(uint32_t n_epochs, const uint32_t* epoch_masks)
     const uint32_t* d_ids = nullptr;
     if (n != nchunks) {
       CK(cudaMemcpyAsync(d_chunk_ids[si], ids, n * 4, cudaMemcpyHostToDevice,
-                         s_comp));
+                         s_enc));
       d_ids = d_chunk_ids[si];
     }
     // the aggregation that read this compressed slot two batches ago must
     // be done before the encoders overwrite it
-    CK(cudaStreamWaitEvent(s_comp, ev_agg_done[si], 0));
-    if (timed_begin(s_comp, &metrics.compress, double(n * P.chunk_bytes), 0))
+    CK(cudaStreamWaitEvent(s_enc, ev_agg_done[si], 0));
+    if (timed_begin(s_enc, &metrics.compress, double(n * P.chunk_bytes), 0))
       return 1;
-    if (codec_compress(n, d_ids, d_comp[si], d_sizes[si]))
+    if (codec_compress(comp, n, d_ids, d_comp[si], d_sizes[si], s_enc))
       return 1;
-    if (timed_end(s_comp))
+    if (timed_end(s_enc))
       return 1;
     comp = d_comp[si];
   }
@@ -678,9 +713,9 @@ int Stream::kick_batch(uint32_t n_epochs, const uint32_t* epoch_masks)
       uint32_t* hp = h_lut_stage[si][l] + n;
       build_luts(l, na, eps, hg, hp);
       CK(cudaMemcpyAsync(d_gather_tmp[si][l], hg, n * 4, cudaMemcpyHostToDevice,
-                         s_comp));
+                         su));
       CK(cudaMemcpyAsync(d_perm_tmp[si][l], hp, n * 4, cudaMemcpyHostToDevice,
-                         s_comp));
+                         su));
       g = d_gather_tmp[si][l];
       pm = d_perm_tmp[si][l];
     }
@@ -693,7 +728,9 @@ int Stream::kick_batch(uint32_t n_epochs, const uint32_t* epoch_masks)
     DeliverySlot::Level& D = S.lv[l];
     A.offsets = D.offsets;
     A.real_sizes = D.real_sizes;
-    A.out = D.data;
+    A.out = D.d_data ? D.d_data : D.data;
+    D.positions = A.positions;
+    D.copied = 0;
     S.level_of[S.n_levels++] = l;
   }
   // zero-copy writes handed to the sink from this slot must have retired
@@ -706,14 +743,23 @@ int Stream::kick_batch(uint32_t n_epochs, const uint32_t* epoch_masks)
   // input reads the chunk pool itself and stays in order on the compute
   // stream.
   cudaStream_t sa = s_comp;
-  if (cfg.codec.id != CODEC_NONE) {
-    CK(cudaEventRecord(ev_codec_done[si], s_comp));
+  if (coded) {
+    CK(cudaEventRecord(ev_codec_done[si], s_enc));
     CK(cudaStreamWaitEvent(s_agg, ev_codec_done[si], 0));
     sa = s_agg;
   }
   if (timed_begin(sa, &metrics.aggregate, 0, 0))
     return 1;
   CK(launch_aggregate(ab, d_agg_scratch + si * agg_scratch_slot, sa));
+  // to the host: the expected bytes now, the rest (if any) at delivery
+  for (int k = 0; k < S.n_levels; ++k) {
+    DeliverySlot::Level& D = S.lv[S.level_of[k]];
+    if (!D.d_data)
+      continue;
+    D.copied = std::min(agg_estimate[S.level_of[k]], D.data_cap);
+    if (D.copied)
+      CK(cudaMemcpyAsync(D.data, D.d_data, D.copied, cudaMemcpyDeviceToHost, sa));
+  }
   if (timed_end(sa))
     return 1;
   CK(cudaEventRecord(ev_agg_done[si], sa));
@@ -723,6 +769,7 @@ int Stream::kick_batch(uint32_t n_epochs, const uint32_t* epoch_masks)
   S.epoch_done_ms.swap(pending_epoch_ms);
   pending_epoch_ms.clear();
   next_slot ^= 1;
+  pool_claimed = false;
   return 0;
 }
 
@@ -736,6 +783,17 @@ int Stream::deliver(int si)
   CK(cudaEventSynchronize(ev_batch[si]));
   S.busy = 0;
   resolve_timers(false);
+  for (int k = 0; k < S.n_levels; ++k) {
+    const int l = S.level_of[k];
+    DeliverySlot::Level& D = S.lv[l];
+    if (!D.d_data)
+      continue;
+    const uint64_t total = D.offsets[D.positions];
+    if (total > D.copied) // more than expected: copy the rest now
+      CK(cudaMemcpy(D.data + D.copied, D.d_data + D.copied, total - D.copied,
+                    cudaMemcpyDeviceToHost));
+    agg_estimate[l] = total + total / 32 + (16u << 10);
+  }
   const double t0 = now_ms();
   uint64_t bytes_out = 0;
   const uint64_t sa = cfg.shard_alignment;
@@ -928,6 +986,8 @@ int Stream::flush_all()
     uint32_t drain = 0;
     for (int l = 1; l < P.nlod; ++l)
       if (counts[l] > 0) {
+        if (claim_pool())
+          return 1;
         if (lod_tiled) {
           LodTileArgs t = tile;
           t.slot = pool_slot(0);
@@ -1082,6 +1142,7 @@ tile_stream_gpu_restart(tile_stream_gpu* s, shard_sink* sink)
   if (I.cursor != 0 && !I.flushed)
     return 1;
   if (cudaStreamSynchronize(I.s_comp) != cudaSuccess ||
+      cudaStreamSynchronize(I.s_enc) != cudaSuccess ||
       cudaStreamSynchronize(I.s_agg) != cudaSuccess ||
       cudaStreamSynchronize(I.s_copy) != cudaSuccess)
     return 1;

@@ -31,8 +31,11 @@ struct DeliverySlot
   {
     uint64_t* offsets = nullptr;    // [positions + 1]
     uint64_t* real_sizes = nullptr; // [positions]
-    uint8_t* data = nullptr;
+    uint8_t* data = nullptr;        // host (mapped) shard-ordered bytes
+    uint8_t* d_data = nullptr;      // device copy (compressed codecs)
     uint64_t positions_cap = 0, data_cap = 0;
+    uint64_t positions = 0;         // of the batch in the slot
+    uint64_t copied = 0;            // bytes already copied to the host
   };
   Level lv[LOD_MAX_LEVELS];
   uint32_t active[LOD_MAX_LEVELS] = {};
@@ -59,8 +62,14 @@ struct Stream
   int in_buf = 0;
   uint64_t in_fill = 0;
 
-  // chunk pool / compression
+  // chunk pool / compression.  With a codec the pool has two halves, one
+  // per delivery slot: the LOD of the next batch fills one half while the
+  // encoders (on their own stream) read the other.
   uint8_t* d_pool = nullptr;
+  uint64_t pool_half_bytes = 0; // 0: one pool (no codec)
+  bool pool_claimed = false;    // the filling half waited for its last encode
+  cudaStream_t s_enc = nullptr; // encoders
+  cudaEvent_t ev_pool_ready = nullptr;
   uint8_t* d_comp[2] = {}; // compressed slots, one per delivery slot
   cudaStream_t s_agg = nullptr; // aggregation (host-link bound) stream
   cudaEvent_t ev_codec_done[2] = {}, ev_agg_done[2] = {};
@@ -102,6 +111,9 @@ struct Stream
   uint32_t lut_cap[LOD_MAX_LEVELS] = {};
   uint32_t planned_count[LOD_MAX_LEVELS] = {};
   uint64_t* d_agg_scratch = nullptr;
+  // bytes per level copied device -> host with the batch (the rest, if
+  // any, at delivery): the last batch's size plus a margin
+  uint64_t agg_estimate[LOD_MAX_LEVELS] = {};
   uint64_t agg_scratch_slot = 0; // entries per delivery slot
   DeliverySlot slot[2];
   cudaEvent_t ev_batch[2] = {};
@@ -145,6 +157,7 @@ struct Stream
                   uint32_t* gather,
                   uint32_t* perm) const;
   uint8_t* pool_slot(uint32_t e) const;
+  int claim_pool();
   int run_epoch(uint64_t present);
   int kick_batch(uint32_t n_epochs, const uint32_t* epoch_masks);
   int batch_boundary();
@@ -156,10 +169,12 @@ struct Stream
   writer_result flush();
 
   int codec_init();
-  int codec_compress(uint64_t nchunks,
+  int codec_compress(const uint8_t* pool,
+                     uint64_t nchunks,
                      const uint32_t* d_ids,
                      uint8_t* out,
-                     uint64_t* sizes);
+                     uint64_t* sizes,
+                     cudaStream_t st);
   void codec_release();
 
   int timed_begin(cudaStream_t st, stream_metric* m, double in, double out);
