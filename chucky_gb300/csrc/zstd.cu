@@ -437,6 +437,8 @@ struct WeightChain
 {
   uint16_t enc[256]; // per step: low bits | bit count << 8
   uint32_t nsteps, ncount_len, fin1, fin2, maxw, warp_bits[8];
+  uint32_t high;            // highest position of the regular symbols
+  uint32_t spread_ballot0;  // valid walk positions among the first 32
 };
 
 // ---------------------------------------------------------------------------
@@ -735,38 +737,90 @@ __device__ void huff_describe(TableShared& T, int tid)
   __syncthreads();
   constexpr int al = 6;
   uint8_t* out = h.desc + 1;
+  const int nsym = int(c.maxw) + 2 <= 13 ? int(c.maxw) + 2 : 13; // room for a spare symbol
+  constexpr int size = 1 << al;
+  FseEnc& t = T.tw;
   if (tid == 0) {
-    const int nsym = int(c.maxw) + 2 <= 13 ? int(c.maxw) + 2 : 13; // room for a spare symbol
     norm_weights(x.whist, nsym, al, x.norm);
-    fse_build(T.tw, x.norm, nsym, al, x.spread, x.fill);
+    // counts, first states, and the top positions of "less than 1" symbols
+    int acc = 0, high = size - 1;
+    for (int sy = 0; sy < nsym; ++sy) {
+      t.count[sy] = x.norm[sy] == -1 ? 1 : x.norm[sy];
+      t.first[sy] = uint8_t(acc);
+      acc += t.count[sy];
+      if (x.norm[sy] == -1)
+        x.spread[high--] = uint8_t(sy);
+    }
+    c.high = uint32_t(high);
+    t.al = al;
     c.ncount_len = uint32_t(write_ncount(out, x.norm, nsym, al));
-    // the two state chains, last weight first; record each step's bits
+    c.nsteps = uint32_t(nw - 2);
+  }
+  __syncthreads();
+  // The symbol spread of fse_build in parallel: position j of the walk
+  // (j * step mod size) is the rank-th valid one (<= high), and the rank-th
+  // valid position goes to the symbol whose cumulative count covers it.
+  constexpr int step = (size >> 1) + (size >> 3) + 3;
+  static_assert(size == 64, "two warps walk the table");
+  if (warp == 0) { // valid walk positions among the first 32
+    const uint32_t pos = uint32_t(tid * step) & (size - 1);
+    const unsigned m = __ballot_sync(0xffffffffu, pos <= c.high);
+    if (lane == 0)
+      c.spread_ballot0 = m;
+  }
+  __syncthreads();
+  if (tid < size) {
+    const uint32_t pos = uint32_t(tid * step) & (size - 1);
+    const bool valid = pos <= c.high;
+    const unsigned m = __ballot_sync(0xffffffffu, valid);
+    const uint32_t rank =
+      __popc(m & ((1u << lane) - 1)) + (warp == 1 ? __popc(c.spread_ballot0) : 0);
+    if (valid) {
+      int sy = 0;
+      uint32_t cum = 0;
+      for (; sy < nsym; ++sy) {
+        const uint32_t n = x.norm[sy] > 0 ? uint32_t(x.norm[sy]) : 0;
+        if (rank < cum + n)
+          break;
+        cum += n;
+      }
+      x.spread[pos] = uint8_t(sy);
+    }
+  }
+  __syncthreads();
+  // states of each symbol in increasing position order
+  if (tid < size) {
+    const int sy = x.spread[tid];
+    int before = 0;
+    for (int u = 0; u < tid; ++u)
+      before += x.spread[u] == sy;
+    t.states[t.first[sy] + before] = uint8_t(tid);
+  }
+  __syncthreads();
+  // The two interleaved state chains, last weight first, one lane each:
+  // the chain initialised with weight nw-1 encodes the even steps (weights
+  // nw-3, nw-5, ...), the one initialised with weight nw-2 the odd steps
+  // (nw-4, nw-6, ...).  Each step's bits are recorded for the packing
+  // below.  The stream closes with state 2 then state 1, where state 1 is
+  // the even-step chain when nw is odd and the odd-step chain when even.
+  if (tid < 2) {
     const FseEnc& t = T.tw;
-    uint32_t v1, v2;
-    int i = nw, k = 0;
-    auto step = [&](uint32_t& v, int s) {
+    const int par = tid; // 0: even steps, 1: odd steps
+    uint32_t v = fse_init(t, w[nw - 1 - par]);
+    for (int k = par, idx = nw - 3 - par; idx >= 0; k += 2, idx -= 2) {
+      const int s = w[idx];
       const int cnt = t.count[s];
       int nb = al - highbit(uint32_t(cnt));
       if ((v >> nb) < uint32_t(cnt))
         --nb;
-      c.enc[k++] = uint16_t((v & ((1u << nb) - 1)) | (uint32_t(nb) << 8));
+      c.enc[k] = uint16_t((v & ((1u << nb) - 1)) | (uint32_t(nb) << 8));
       v = t.states[t.first[s] + ((v >> nb) - cnt)] + (1u << al);
-    };
-    if (nw & 1) {
-      v1 = fse_init(t, w[--i]);
-      v2 = fse_init(t, w[--i]);
-      step(v1, w[--i]);
-    } else {
-      v2 = fse_init(t, w[--i]);
-      v1 = fse_init(t, w[--i]);
     }
-    while (i > 0) {
-      step(v2, w[--i]);
-      step(v1, w[--i]);
-    }
-    c.nsteps = uint32_t(k);
-    c.fin1 = v1 - (1u << al);
-    c.fin2 = v2 - (1u << al);
+    const bool state1 = (nw & 1) ? par == 0 : par == 1;
+    if (state1)
+      c.fin1 = v - (1u << al);
+    else
+      c.fin2 = v - (1u << al);
   }
   __syncthreads();
   // pack: thread k writes step k's bits at the sum of the steps before it

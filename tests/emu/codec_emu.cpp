@@ -48,6 +48,10 @@ static void fill(uint8_t* p, size_t n, const std::string& pat, size_t chunk)
       p[i] = 0;
     else if (pat == "random")
       p[i] = uint8_t(rnd());
+    else if (pat == "u200") // values 0..199: an even count of explicit weights
+      p[i] = uint8_t(rnd() % 200);
+    else if (pat == "u201") // values 0..200: an odd count
+      p[i] = uint8_t(rnd() % 201);
     else if (pat == "geom") { // skewed: P(k) ~ 2^-(k+1), rare other bytes
       const uint64_t r = rnd();
       p[i] = (r & 511) == 0 ? uint8_t(r >> 9) : uint8_t(__builtin_ctzll(r | (1ull << 40)));

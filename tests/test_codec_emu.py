@@ -37,7 +37,10 @@ CASES = [(1024, 6), (37, 3), (13, 2), (1, 2)]
 BIG = [("zstd", "xor16", 200000, 1), ("zstd", "mixed", 131072, 2),
        ("lz4", "xor16", 140000, 1), ("lz4", "mixed", 65536, 2),
        # skewed bytes: Huffman depths beyond the 11-bit limit get repaired
-       ("zstd", "geom", 40000, 1), ("lz4", "geom", 9000, 1)]
+       ("zstd", "geom", 40000, 1), ("lz4", "geom", 9000, 1),
+       # FSE-coded Huffman weights (more than 128), both parities of their
+       # count (the two interleaved state chains end on either state)
+       ("zstd", "u200", 70000, 1), ("zstd", "u201", 70000, 1)]
 
 
 def _run(emu, codec, pattern, chunk, n):
