@@ -397,7 +397,7 @@ tile_stream_gpu_memory_estimate(const tile_stream_configuration* config,
       scratch = chucky::zstd_scratch_bytes(wave, uint32_t(P.chunk_bytes));
     else if (config->codec.id == CODEC_LZ4_NON_STANDARD)
       scratch = chucky::lz4_scratch_bytes(wave, uint32_t(P.chunk_bytes));
-    info->codec_bytes = 2 * nchunks * 8 + scratch;
+    info->codec_bytes = 2 * nchunks * 8 + 2 * scratch; // one scratch per slot
   }
   info->shard_bytes = shard;
   info->device_bytes = info->staging_bytes + info->chunk_pool_bytes +

@@ -31,7 +31,10 @@ int Stream::codec_init()
     if (cudaMallocHost(&h_chunk_ids[i], n * 4) != cudaSuccess ||
         cudaMalloc(&d_chunk_ids[i], n * 4) != cudaSuccess)
       return 1;
-  return cudaMalloc(&codec_state, bytes) == cudaSuccess ? 0 : 1;
+  for (int i = 0; i < 2; ++i)
+    if (cudaMalloc(&codec_state[i], bytes) != cudaSuccess)
+      return 1;
+  return 0;
 }
 
 int Stream::codec_compress(const uint8_t* pool,
@@ -39,6 +42,7 @@ int Stream::codec_compress(const uint8_t* pool,
                            const uint32_t* d_ids,
                            uint8_t* out,
                            uint64_t* sizes,
+                           void* scratch,
                            cudaStream_t st)
 {
   cudaError_t e = cudaSuccess;
@@ -61,8 +65,8 @@ int Stream::codec_compress(const uint8_t* pool,
       b.out = out + first * comp_stride;
       b.out_sizes = sizes + first;
     }
-    e = cfg.codec.id == CODEC_ZSTD ? launch_zstd(b, codec_state, st)
-                                   : launch_lz4(b, codec_state, st);
+    e = cfg.codec.id == CODEC_ZSTD ? launch_zstd(b, scratch, st)
+                                   : launch_lz4(b, scratch, st);
   }
   if (e != cudaSuccess) {
     std::fprintf(stderr, "chucky_gb300: %s encoder launch failed: %s\n",
@@ -75,8 +79,10 @@ int Stream::codec_compress(const uint8_t* pool,
 
 void Stream::codec_release()
 {
-  cudaFree(codec_state);
-  codec_state = nullptr;
+  for (int i = 0; i < 2; ++i) {
+    cudaFree(codec_state[i]);
+    codec_state[i] = nullptr;
+  }
   for (int i = 0; i < 2; ++i) {
     cudaFreeHost(h_chunk_ids[i]);
     cudaFree(d_chunk_ids[i]);

@@ -127,7 +127,8 @@ int Stream::init(const tile_stream_configuration* c, shard_sink* sk)
   CK(cudaStreamCreateWithFlags(&s_copy, cudaStreamNonBlocking));
   CK(cudaStreamCreateWithFlags(&s_comp, cudaStreamNonBlocking));
   CK(cudaStreamCreateWithFlags(&s_agg, cudaStreamNonBlocking));
-  CK(cudaStreamCreateWithFlags(&s_enc, cudaStreamNonBlocking));
+  for (int i = 0; i < 2; ++i)
+    CK(cudaStreamCreateWithFlags(&s_enc[i], cudaStreamNonBlocking));
   CK(cudaEventCreateWithFlags(&ev_pool_ready, cudaEventDisableTiming));
   for (auto& t : timers) {
     CK(cudaEventCreate(&t.a));
@@ -140,7 +141,7 @@ int Stream::init(const tile_stream_configuration* c, shard_sink* sk)
     CK(cudaEventCreateWithFlags(&ev_codec_done[i], cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&ev_agg_done[i], cudaEventDisableTiming));
     CK(cudaEventRecord(ev_agg_done[i], s_comp));
-    CK(cudaEventRecord(ev_codec_done[i], s_enc));
+    CK(cudaEventRecord(ev_codec_done[i], s_enc[i]));
     CK(cudaMalloc(&d_epoch[i], round_up(P.epoch_bytes, 256) + 256));
     CK(cudaEventRecord(ev_input_free[i], s_comp));
   }
@@ -448,8 +449,9 @@ void Stream::release()
 {
   if (s_comp)
     cudaStreamSynchronize(s_comp);
-  if (s_enc)
-    cudaStreamSynchronize(s_enc);
+  for (cudaStream_t e : s_enc)
+    if (e)
+      cudaStreamSynchronize(e);
   if (s_agg)
     cudaStreamSynchronize(s_agg);
   if (s_copy)
@@ -486,8 +488,9 @@ void Stream::release()
   }
   if (s_agg)
     cudaStreamDestroy(s_agg);
-  if (s_enc)
-    cudaStreamDestroy(s_enc);
+  for (cudaStream_t e : s_enc)
+    if (e)
+      cudaStreamDestroy(e);
   if (ev_pool_ready)
     cudaEventDestroy(ev_pool_ready);
   if (d_sizes[1] != d_sizes[0])
@@ -651,11 +654,12 @@ int Stream::kick_batch(uint32_t n_epochs, const uint32_t* epoch_masks)
   const uint8_t* comp = d_pool + si * pool_half_bytes;
   const bool coded = cfg.codec.id != CODEC_NONE;
   // the aggregation's LUT uploads ride on the stream that precedes it
-  const cudaStream_t su = coded ? s_enc : s_comp;
+  const cudaStream_t se = s_enc[si];
+  const cudaStream_t su = coded ? se : s_comp;
   if (coded) {
     // the encoders start once this batch's pool half is filled
     CK(cudaEventRecord(ev_pool_ready, s_comp));
-    CK(cudaStreamWaitEvent(s_enc, ev_pool_ready, 0));
+    CK(cudaStreamWaitEvent(se, ev_pool_ready, 0));
     // encode only the chunks of active (epoch, level) pairs
     uint32_t* ids = h_chunk_ids[si];
     uint64_t n = 0;
@@ -669,17 +673,17 @@ int Stream::kick_batch(uint32_t n_epochs, const uint32_t* epoch_masks)
     const uint32_t* d_ids = nullptr;
     if (n != nchunks) {
       CK(cudaMemcpyAsync(d_chunk_ids[si], ids, n * 4, cudaMemcpyHostToDevice,
-                         s_enc));
+                         se));
       d_ids = d_chunk_ids[si];
     }
     // the aggregation that read this compressed slot two batches ago must
     // be done before the encoders overwrite it
-    CK(cudaStreamWaitEvent(s_enc, ev_agg_done[si], 0));
-    if (timed_begin(s_enc, &metrics.compress, double(n * P.chunk_bytes), 0))
+    CK(cudaStreamWaitEvent(se, ev_agg_done[si], 0));
+    if (timed_begin(se, &metrics.compress, double(n * P.chunk_bytes), 0))
       return 1;
-    if (codec_compress(comp, n, d_ids, d_comp[si], d_sizes[si], s_enc))
+    if (codec_compress(comp, n, d_ids, d_comp[si], d_sizes[si], codec_state[si], se))
       return 1;
-    if (timed_end(s_enc))
+    if (timed_end(se))
       return 1;
     comp = d_comp[si];
   }
@@ -744,7 +748,7 @@ int Stream::kick_batch(uint32_t n_epochs, const uint32_t* epoch_masks)
   // stream.
   cudaStream_t sa = s_comp;
   if (coded) {
-    CK(cudaEventRecord(ev_codec_done[si], s_enc));
+    CK(cudaEventRecord(ev_codec_done[si], se));
     CK(cudaStreamWaitEvent(s_agg, ev_codec_done[si], 0));
     sa = s_agg;
   }
@@ -1142,7 +1146,8 @@ tile_stream_gpu_restart(tile_stream_gpu* s, shard_sink* sink)
   if (I.cursor != 0 && !I.flushed)
     return 1;
   if (cudaStreamSynchronize(I.s_comp) != cudaSuccess ||
-      cudaStreamSynchronize(I.s_enc) != cudaSuccess ||
+      cudaStreamSynchronize(I.s_enc[0]) != cudaSuccess ||
+      cudaStreamSynchronize(I.s_enc[1]) != cudaSuccess ||
       cudaStreamSynchronize(I.s_agg) != cudaSuccess ||
       cudaStreamSynchronize(I.s_copy) != cudaSuccess)
     return 1;

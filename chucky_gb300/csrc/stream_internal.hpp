@@ -64,18 +64,19 @@ struct Stream
 
   // chunk pool / compression.  With a codec the pool has two halves, one
   // per delivery slot: the LOD of the next batch fills one half while the
-  // encoders (on their own stream) read the other.
+  // encoders of the previous one read the other.  Each slot has its own
+  // encoder stream and scratch, so consecutive batches' encoders overlap.
   uint8_t* d_pool = nullptr;
   uint64_t pool_half_bytes = 0; // 0: one pool (no codec)
   bool pool_claimed = false;    // the filling half waited for its last encode
-  cudaStream_t s_enc = nullptr; // encoders
+  cudaStream_t s_enc[2] = {}; // encoders, one stream per delivery slot
   cudaEvent_t ev_pool_ready = nullptr;
   uint8_t* d_comp[2] = {}; // compressed slots, one per delivery slot
   cudaStream_t s_agg = nullptr; // aggregation (host-link bound) stream
   cudaEvent_t ev_codec_done[2] = {}, ev_agg_done[2] = {};
   uint64_t* d_sizes[2] = {}; // compressed sizes, one per delivery slot
   uint64_t comp_stride = 0;
-  void* codec_state = nullptr;
+  void* codec_state[2] = {}; // encoder scratch, one per delivery slot
   uint64_t wave_chunks = 0; // chunks per encoder launch
   uint32_t* h_chunk_ids[2] = {};   // pinned staging of the encode list
   uint32_t* d_chunk_ids[2] = {};
@@ -174,6 +175,7 @@ struct Stream
                      const uint32_t* d_ids,
                      uint8_t* out,
                      uint64_t* sizes,
+                     void* scratch,
                      cudaStream_t st);
   void codec_release();
 
