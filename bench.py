@@ -74,6 +74,101 @@ WORKLOAD = ("256^3 u16 (mean LOD) + 256^3 f32 (median LOD), chunk 64^3, shard "
             "4^3 chunks, 2x2x2 pyramid (3 levels), zstd-3, K=%d epochs per batch "
             "(%d batches per array), discard sink" % (EPOCHS_PER_BATCH, 4 // EPOCHS_PER_BATCH))
 
+# Further workloads (`--workload`), each printing its own line; the default
+# line is the plain multiscale one above.
+SENSOR_H, SENSOR_W = 2304, 4096
+
+
+def sensor_frames(nframes, dev, seed=11):
+    """u16 sensor frames 2304 x 4096: Poisson(100) background plus 64 seeded
+    2-D Gaussian blobs (sigma 4-20 px, peak 500-4000), clipped to 12 bits.
+    Generated on the device (seeded torch generator); returns an int16
+    (nframes, H, W) device tensor whose bytes are the u16 little-endian
+    frames (values <= 4095)."""
+    import torch
+    rng = np.random.default_rng(seed)
+    yy = torch.arange(SENSOR_H, device=dev, dtype=torch.float32)[:, None]
+    xx = torch.arange(SENSOR_W, device=dev, dtype=torch.float32)[None, :]
+    rate = torch.full((SENSOR_H, SENSOR_W), 100.0, device=dev)
+    for _ in range(64):
+        cy, cx = rng.uniform(0, SENSOR_H), rng.uniform(0, SENSOR_W)
+        s, a = rng.uniform(4, 20), rng.uniform(500, 4000)
+        rate += a * torch.exp(-((yy - cy) ** 2 + (xx - cx) ** 2) / (2 * s * s))
+    g = torch.Generator(device=dev)
+    g.manual_seed(seed)
+    out = torch.empty((nframes, SENSOR_H, SENSOR_W), dtype=torch.int16, device=dev)
+    for f0 in range(0, nframes, 16):
+        n = min(16, nframes - f0)
+        r = rate.expand(n, SENSOR_H, SENSOR_W).contiguous()
+        out[f0:f0 + n] = torch.poisson(r, generator=g).clamp_(max=4095).to(torch.int16)
+    return out
+
+
+def sensor_config(codec, reduce):
+    """Unbounded dim 0 (chunk 32 frames), chunk 32 x 256 x 256, shard
+    32 x 2048 x 2048, (t, y, x) pyramid of 5 levels with dim-0
+    downsampling."""
+    dims = capi.make_dims([
+        dict(size=0, chunk=32, cps=1, downsample=1, name="t"),
+        dict(size=SENSOR_H, chunk=256, cps=8, downsample=1, name="y"),
+        dict(size=SENSOR_W, chunk=256, cps=8, downsample=1, name="x")])
+    cfg = capi.make_config(dims, dtype="u16", codec=codec, level=1, reduce=reduce,
+                           append_reduce=reduce, max_nlod=5,
+                           epochs_per_batch=EPOCHS_PER_BATCH,
+                           buffer_capacity_bytes=128 << 20)
+    cfg._dims = dims
+    return cfg
+
+
+def cube_lz4_config():
+    dims = capi.make_dims([dict(size=SIDE, chunk=CHUNK, cps=4, name=n) for n in "zyx"])
+    cfg = capi.make_config(dims, dtype="u16", codec="lz4", level=1,
+                           epochs_per_batch=EPOCHS_PER_BATCH,
+                           buffer_capacity_bytes=128 << 20)
+    cfg._dims = dims
+    return cfg
+
+
+def make_workload(name, dev, frames):
+    """(description, data note, dtype, [(config, pinned host bytes, device
+    bytes)], encoder name) of a workload."""
+    import torch
+
+    def pair(dbuf):
+        dbuf = dbuf.reshape(-1).view(torch.uint8)
+        host = torch.empty(dbuf.numel(), dtype=torch.uint8, pin_memory=True)
+        host.copy_(dbuf)
+        return host, dbuf
+
+    if name == "multiscale":
+        u16, f32 = make_cubes()
+        arrays = []
+        for cube, cfg in ((u16, make_config("u16", "mean")), (f32, make_config("f32", "median"))):
+            host = torch.from_numpy(cube.reshape(-1).view(np.uint8)).pin_memory()
+            arrays.append((cfg, host, host.to(dev)))
+        return (WORKLOAD, "synthetic (seeded xor+noise u16 cube, sin*cos f32 cube + N(0,0.01))",
+                "u16+f32", arrays, "zstd encoder (find+table+block+frame)")
+    if name == "cube-lz4":
+        u16, _ = make_cubes()
+        host = torch.from_numpy(u16.reshape(-1).view(np.uint8)).pin_memory()
+        desc = ("256^3 u16, chunk 64^3, shard 4^3 chunks (one shard), no LOD, LZ4, "
+                "K=%d epochs per batch, discard sink" % EPOCHS_PER_BATCH)
+        return (desc, "synthetic (seeded xor+noise u16 cube)", "u16",
+                [(cube_lz4_config(), host, host.to(dev))], "lz4 encoder (find+plan+emit)")
+    if name in ("sensor-zstd", "sensor-lz4"):
+        codec = name.split("-")[1]
+        host, dbuf = pair(sensor_frames(frames, dev))
+        desc = ("%d u16 frames 2304x4096 along unbounded dim 0, chunk 32x256x256, shard "
+                "32x2048x2048, (t,y,x) max pyramid (5 levels, dim-0 downsampling), %s, "
+                "K=%d epochs per batch, discard sink"
+                % (frames, "zstd-1" if codec == "zstd" else "LZ4", EPOCHS_PER_BATCH))
+        enc = ("zstd encoder (find+table+block+frame)" if codec == "zstd"
+               else "lz4 encoder (find+plan+emit)")
+        return (desc, "synthetic (seeded Poisson(100) + 64 Gaussian blobs, 12-bit; "
+                "generated on the device)", "u16",
+                [(sensor_config(codec, "max"), host, dbuf)], enc)
+    raise ValueError(name)
+
 
 class Clocks:
     """nvidia-smi samples during the timed region."""
@@ -140,6 +235,24 @@ def max_over_ranks(values, world, device):
     return [float(v) for v in t.tolist()]
 
 
+def h2d_probe(host, devbuf, dev, reps=3):
+    """GB/s of plain pinned host -> device copies of the input buffers."""
+    import torch
+    s = torch.cuda.Stream(device=dev)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    with torch.cuda.stream(s):
+        e0.record(s)
+        for _ in range(reps):
+            for h, d in zip(host, devbuf):
+                d.copy_(h, non_blocking=True)
+        e1.record(s)
+    s.synchronize()
+    nbytes = reps * sum(h.numel() for h in host)
+    return nbytes / (e0.elapsed_time(e1) * 1e-3) / 1e9
+
+
 def whole_job_gbs(bytes_per_rank_step, steps, world, ms):
     """Input GB/s of the whole job: every rank ingests its own replica."""
     return bytes_per_rank_step * steps * world / (ms * 1e-3) / 1e9
@@ -161,13 +274,13 @@ def run_ours(args, rank, world):
     dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
     torch.cuda.set_device(dev)
 
-    u16, f32 = make_cubes()
-    host = [torch.from_numpy(a.reshape(-1).view(np.uint8)).pin_memory() for a in (u16, f32)]
-    devbuf = [h.to(dev) for h in host]
+    desc, data_note, dtype_name, arrays, enc_name = make_workload(args.workload, dev,
+                                                                  args.frames)
+    host = [a[1] for a in arrays]
+    devbuf = [a[2] for a in arrays]
     nbytes = sum(h.numel() for h in host)
     sink = lib.chucky_discard_sink_create()
-    cfgs = [make_config("u16", "mean"), make_config("f32", "median")]
-    streams = [cg.GpuStream(c, sink) for c in cfgs]
+    streams = [cg.GpuStream(a[0], sink) for a in arrays]
     flush_buf = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
 
     def step(bufs):
@@ -221,8 +334,12 @@ def run_ours(args, rank, world):
     if rank == 0:
         clocks.start()
     times_dev, m0, m1, sink_b, launches = timed(devbuf, args.steps, args.warmup)
-    times_host, _, _, sink_h, launches_h = timed(host, args.steps, max(1, args.warmup // 2))
+    times_host, m0h, m1h, sink_h, launches_h = timed(host, args.steps, max(1, args.warmup // 2))
     clk = clocks.stop() if rank == 0 else None
+    # the host link as the e2e leg sees it: plain copies of the same pinned
+    # input buffers to the device, right after the timed region (the link
+    # and host memory are shared with other tenants of the machine)
+    link_gbs = h2d_probe(host, devbuf, dev)
 
     ms_dev, ms_host = max_over_ranks([float(np.sum(times_dev)), float(np.sum(times_host))],
                                      world, dev)
@@ -237,7 +354,7 @@ def run_ours(args, rank, world):
     per_launch_bytes = comp_in / max(1, comp_launches)
     # DRAM bytes (read + written) per byte of encoder input, measured by ncu
     # on one batch of the u16 cube: 55.1 MB for 19.40 MB of chunk input
-    traffic_per_input_byte = 2.84
+    traffic_per_input_byte = 2.84 if args.workload == "multiscale" else None
     peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     peak, peak_src = 6800.0, "fallback"
     if os.path.exists(peaks_path):
@@ -249,11 +366,15 @@ def run_ours(args, rank, world):
     out_per_launch = sink_b / max(1.0, launches_per_step)
     achieved = ((per_launch_bytes + out_per_launch) / (per_launch_ms * 1e-3) / 1e9
                 if per_launch_ms > 0 else 0.0)
-    stages = {}
-    for name in capi.METRIC_NAMES:
-        ms = sum(getattr(b, name).ms - getattr(a, name).ms for a, b in zip(m0, m1))
-        if ms > 0:
-            stages[name] = round(ms / args.steps, 4)
+    def stage_ms(a0, a1):
+        out = {}
+        for name in capi.METRIC_NAMES:
+            ms = sum(getattr(b, name).ms - getattr(a, name).ms for a, b in zip(a0, a1))
+            if ms > 0:
+                out[name] = round(ms / args.steps, 4)
+        return out
+
+    stages, stages_e2e = stage_ms(m0, m1), stage_ms(m0h, m1h)
 
     for s in streams:
         s.close()
@@ -264,31 +385,38 @@ def run_ours(args, rank, world):
         "metric": METRIC, "value": round(value, 3), "unit": "GB/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(ms_dev / args.steps, 4), "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "u16+f32",
-        "data": "synthetic (seeded xor+noise u16 cube, sin*cos f32 cube + N(0,0.01))",
-        "config": {"workload": WORKLOAD, "input_bytes_per_step": nbytes,
+        "scaling": "weak", "vs_baseline": None, "dtype": dtype_name,
+        "data": data_note,
+        "config": {"workload": desc, "input_bytes_per_step": nbytes,
                    "l2": "flushed between steps (256 MiB write)",
                    "parallelism": f"replicas x{world}",
                    "stage_ms_per_step": stages},
         "e2e": {"value": round(e2e, 3), "unit": "GB/s",
                 "h2d_bytes_per_step": nbytes,
                 "d2h_bytes_per_step": int(sink_h),
-                "ms_per_step": round(ms_host / args.steps, 4)},
+                "ms_per_step": round(ms_host / args.steps, 4),
+                "stage_ms_per_step": stages_e2e,
+                # pinned H2D copies of the same input buffers, measured
+                # right after the timed region
+                "h2d_link_gbs": round(link_gbs, 2),
+                "frac_of_h2d_link": round(e2e / link_gbs, 4) if link_gbs else None},
         # delivered chunk bytes (every pyramid level) / compressed shard bytes
         "compression_ratio": round(comp_in / args.steps / max(1.0, sink_b), 4),
-        "roofline": {"kernel": "zstd encoder (find+block+frame)", "bound": "hbm",
+        "roofline": {"kernel": enc_name, "bound": "hbm",
                      "achieved": round(achieved, 2), "peak": peak,
                      "unit": "GB/s", "frac": round(achieved / peak, 4),
                      "peak_source": peak_src,
-                     "traffic": round(traffic_per_input_byte * per_launch_bytes),
+                     "traffic": round(traffic_per_input_byte * per_launch_bytes)
+                     if traffic_per_input_byte else None,
                      "traffic_note": "bytes per launch set, scaled by input bytes "
-                                     "from the u16 ncu capture",
+                                     "from the u16 ncu capture"
+                     if traffic_per_input_byte else "not captured for this workload",
                      "input_gbs": round(per_launch_bytes / (per_launch_ms * 1e-3) / 1e9, 2)
                      if per_launch_ms > 0 else None},
         "gpu_launches": int(launches),
         "clocks": clk,
     }
-    if args.cpu_baseline:
+    if args.cpu_baseline and args.workload == "multiscale":
         line["cpu_baseline"] = cpu_baseline(args)
     return line
 
@@ -375,10 +503,18 @@ def run_single(args):
     lib.chucky_discard_sink_create.restype = C.c_void_p
     lib.chucky_discard_sink_destroy.argtypes = [C.c_void_p]
     lib.tile_stream_gpu_restart.argtypes = [C.c_void_p, C.c_void_p]
-    u16, f32 = make_cubes()
-    cube = u16 if args.single == "u16" else f32
-    cfg = make_config(args.single, "mean" if args.single == "u16" else "median")
-    buf = torch.from_numpy(cube.reshape(-1).view(np.uint8)).cuda()
+    if args.single in ("u16", "f32"):
+        u16, f32 = make_cubes()
+        cube = u16 if args.single == "u16" else f32
+        cfg = make_config(args.single, "mean" if args.single == "u16" else "median")
+        buf = torch.from_numpy(cube.reshape(-1).view(np.uint8)).cuda()
+    elif args.single == "cube-lz4":
+        u16, _ = make_cubes()
+        cfg = cube_lz4_config()
+        buf = torch.from_numpy(u16.reshape(-1).view(np.uint8)).cuda()
+    else:
+        cfg = sensor_config(args.single.split("-")[1], "max")
+        buf = sensor_frames(args.frames, torch.device("cuda")).reshape(-1).view(torch.uint8)
     sink = lib.chucky_discard_sink_create()
     s = cg.GpuStream(cfg, sink)
     for _ in range(args.steps):
@@ -398,7 +534,15 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
-    ap.add_argument("--single", choices=["u16", "f32"],
+    ap.add_argument("--workload", default="multiscale",
+                    choices=["multiscale", "cube-lz4", "sensor-zstd", "sensor-lz4"],
+                    help="multiscale: the plain multiscale line (default); cube-lz4: "
+                         "the 256^3 u16 cube with LZ4 and no LOD; sensor-*: 2304x4096 "
+                         "u16 frames with a 5-level dim-0 pyramid")
+    ap.add_argument("--frames", type=int, default=512,
+                    help="sensor frames per step (multiple of 32)")
+    ap.add_argument("--single", choices=["u16", "f32", "cube-lz4", "sensor-zstd",
+                                         "sensor-lz4"],
                     help="profiling case: one array's stream, --steps passes, no timing")
     args = ap.parse_args()
     if args.single:

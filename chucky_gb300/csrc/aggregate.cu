@@ -133,7 +133,25 @@ __global__ void fill_u64_k(uint64_t* p, uint64_t v, uint64_t n)
     p[i] = v;
 }
 
+__global__ void stage_copy_k(uint32_t* dst, const uint32_t* src, uint64_t n)
+{
+  for (uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; i < n;
+       i += uint64_t(gridDim.x) * blockDim.x)
+    dst[i] = src[i];
+}
+
 } // namespace
+
+cudaError_t launch_stage_copy(uint32_t* dst, const uint32_t* src, uint64_t n,
+                              cudaStream_t st)
+{
+  if (!n)
+    return cudaSuccess;
+  const uint64_t blocks = (n + 255) / 256;
+  stage_copy_k<<<int(blocks < 152 ? blocks : 152), 256, 0, st>>>(dst, src, n);
+  note_launches(1);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_aggregate(const AggBatch& b,
                              uint64_t* scratch,

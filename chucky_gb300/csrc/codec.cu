@@ -28,7 +28,7 @@ int Stream::codec_init()
   if (P.chunk_bytes >= (uint64_t(1) << 32))
     return 1;
   for (int i = 0; i < 2; ++i)
-    if (cudaMallocHost(&h_chunk_ids[i], n * 4) != cudaSuccess ||
+    if (cudaHostAlloc(&h_chunk_ids[i], n * 4, cudaHostAllocMapped) != cudaSuccess ||
         cudaMalloc(&d_chunk_ids[i], n * 4) != cudaSuccess)
       return 1;
   for (int i = 0; i < 2; ++i)

@@ -138,4 +138,11 @@ cudaError_t launch_aggregate(const AggBatch& b,
 
 cudaError_t launch_fill_u64(uint64_t* p, uint64_t v, uint64_t n, cudaStream_t st);
 
+// n 32-bit words from mapped pinned host memory to the device with SM
+// loads.  Small host-built tables (chunk lists, shard-order tables) travel
+// this way rather than as copy-engine transfers, which would queue behind
+// the large input copies to the device that are in flight at the time.
+cudaError_t launch_stage_copy(uint32_t* dst, const uint32_t* src, uint64_t n,
+                              cudaStream_t st);
+
 } // namespace chucky

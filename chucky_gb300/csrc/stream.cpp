@@ -403,7 +403,7 @@ int Stream::setup_aggregate()
     CK(cudaMalloc(&d_gather[l], lut_n * 4));
     CK(cudaMalloc(&d_perm[l], lut_n * 4));
     for (int si = 0; si < 2; ++si) {
-      CK(cudaMallocHost(&h_lut_stage[si][l], 2 * lut_n * 4));
+      CK(cudaHostAlloc(&h_lut_stage[si][l], 2 * lut_n * 4, cudaHostAllocMapped));
       CK(cudaMalloc(&d_gather_tmp[si][l], lut_n * 4));
       CK(cudaMalloc(&d_perm_tmp[si][l], lut_n * 4));
     }
@@ -672,8 +672,7 @@ int Stream::kick_batch(uint32_t n_epochs, const uint32_t* epoch_masks)
         }
     const uint32_t* d_ids = nullptr;
     if (n != nchunks) {
-      CK(cudaMemcpyAsync(d_chunk_ids[si], ids, n * 4, cudaMemcpyHostToDevice,
-                         se));
+      CK(launch_stage_copy(d_chunk_ids[si], ids, n, se));
       d_ids = d_chunk_ids[si];
     }
     // the aggregation that read this compressed slot two batches ago must
@@ -716,10 +715,8 @@ int Stream::kick_batch(uint32_t n_epochs, const uint32_t* epoch_masks)
       uint32_t* hg = h_lut_stage[si][l];
       uint32_t* hp = h_lut_stage[si][l] + n;
       build_luts(l, na, eps, hg, hp);
-      CK(cudaMemcpyAsync(d_gather_tmp[si][l], hg, n * 4, cudaMemcpyHostToDevice,
-                         su));
-      CK(cudaMemcpyAsync(d_perm_tmp[si][l], hp, n * 4, cudaMemcpyHostToDevice,
-                         su));
+      CK(launch_stage_copy(d_gather_tmp[si][l], hg, n, su));
+      CK(launch_stage_copy(d_perm_tmp[si][l], hp, n, su));
       g = d_gather_tmp[si][l];
       pm = d_perm_tmp[si][l];
     }
@@ -915,12 +912,17 @@ int Stream::drain_all()
 
 int Stream::batch_boundary()
 {
-  // the previous batch is delivered while this one runs on the GPU
+  // The previous batch is delivered while this one runs on the GPU: now if
+  // the GPU is already done with it, otherwise when its slot is needed
+  // again (the next kick, which delivers a busy slot first) or at the
+  // flush.  Not waiting here lets the caller enqueue the next batch's
+  // input copies and LOD while two batches are in flight.
   const int prev = next_slot ^ 1;
   if (kick_batch(accumulated, masks))
     return 1;
   accumulated = 0;
-  if (slot[prev].busy && slot[prev].seq < batch_seq)
+  if (slot[prev].busy && slot[prev].seq < batch_seq &&
+      cudaEventQuery(ev_batch[prev]) == cudaSuccess)
     return deliver(prev);
   return 0;
 }

@@ -50,9 +50,14 @@ constexpr uint32_t kMinHufLits = 64;
 constexpr uint32_t kTreelessMinChunk = 64u << 10;
 constexpr uint32_t kHufMaxBits = 11;
 #ifndef CHUCKY_ZSTD_MIN_MATCH
-#define CHUCKY_ZSTD_MIN_MATCH 6
+#define CHUCKY_ZSTD_MIN_MATCH 8
 #endif
-// matches shorter than this cost more as a sequence than as literals
+// Matches shorter than this cost about as much as a sequence (predefined
+// FSE codes of its three fields plus the offset's extra bits, about 30
+// bits) as their bytes cost as Huffman-coded literals, and every match
+// restarts the dense probing of the parser.  8 bytes: on 12-bit sensor
+// frames the encoders run 1.45x faster with a better ratio than with 6,
+// on the u16/f32 cubes 5 % faster for 0.06 % of ratio.
 constexpr uint32_t kMinMatch = CHUCKY_ZSTD_MIN_MATCH;
 
 // Per chunk: 256 literal counts of a 1-in-4 sample of the literal bytes,
