@@ -42,6 +42,17 @@ struct TileGeom<3>
   static constexpr int log = 4; // 16^3
 };
 
+// parents of levels 1..TL inside one L0 tile: the accumulator values a
+// CTA stages for its dim-0 folds
+template<int D>
+__host__ __device__ constexpr int stage_elems()
+{
+  int n = 0;
+  for (int l = 1; l <= TileGeom<D>::log; ++l)
+    n += 1 << (D * (TileGeom<D>::log - l));
+  return n;
+}
+
 // chunk-pool offset (elements) of LOD coords x at level l (fixed part added
 // by the caller)
 template<int D>
@@ -69,6 +80,8 @@ lod_tile_k(LodTileArgs a)
   T* cur = reinterpret_cast<T*>(smem_raw);    // level l values (TN)
   T* nxt = cur + TN;                          // level 1 values (TN >> D); the
                                               // two regions swap per level
+  constexpr int TS = stage_elems<D>();
+  T* const stage = nxt + (TN >> D); // folded levels' accumulators (TS)
 
   const uint64_t b = blockIdx.y; // fixed-dims slice
   uint32_t tcoord[3] = { 0, 0, 0 };
@@ -82,6 +95,48 @@ lod_tile_k(LodTileArgs a)
   }
   const T* lin = reinterpret_cast<const T*>(a.linear) + a.gather_fixed[b];
   T* slot = reinterpret_cast<T*>(a.slot);
+
+  // ---- accumulators of the levels folded this epoch (dim-0 downsampling),
+  // loaded up front with L0: the CTA waits on global memory once instead of
+  // once per level.  Entry j of the stage is parent j - base(l) of level l
+  // (levels in order, parents row-major in the tile, last dim fastest).
+  constexpr int kPre = (TS + kTileThreads - 1) / kTileThreads;
+  T pre[kPre];
+  uint32_t pre_ok = 0;
+#pragma unroll
+  for (int s = 0; s < kPre; ++s) {
+    const int j = s * kTileThreads + int(threadIdx.x);
+    if (j >= TS)
+      continue;
+    int l = 1, base = 0;
+    while (j - base >= (1 << (D * (TL - l)))) {
+      base += 1 << (D * (TL - l));
+      ++l;
+    }
+    if (l >= a.nlod || !((a.fold_mask >> l) & 1) || a.count[l] == 0)
+      continue;
+    const int plog = TL - l;
+    int r = j - base;
+    uint32_t pc[3];
+#pragma unroll
+    for (int k = D - 1; k >= 0; --k) {
+      pc[k] = uint32_t(r & ((1 << plog) - 1));
+      r >>= plog;
+    }
+    uint64_t ai = 0;
+    bool in = true;
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+      const uint32_t gx = ((tcoord[k] * uint32_t(TE)) >> l) + pc[k];
+      in &= gx < a.lv[l].shape[k];
+      ai = ai * a.lv[l].shape[k] + gx;
+    }
+    if (!in)
+      continue;
+    pre[s] = reinterpret_cast<const T*>(a.accum)[a.lv[l].accum_off +
+                                                 b * a.lv[l].nelem + ai];
+    pre_ok |= 1u << s;
+  }
 
   // ---- L0: load (innermost LOD dim fastest -> coalesced rows) ----
   uint32_t ext[3]; // extent of this tile at the current level (<= edge)
@@ -113,41 +168,85 @@ lod_tile_k(LodTileArgs a)
             (reinterpret_cast<uintptr_t>(lin) & 15) == 0 &&
             (reinterpret_cast<uintptr_t>(slot) & 15) == 0;
   }
-  if (fast) {
-    constexpr int kVec = 16 / int(sizeof(T) > 16 ? 16 : sizeof(T)); // elements per vector
-    constexpr int kVpr = TE / kVec;                                  // vectors per row
-    for (int i = threadIdx.x; i < TE * kVpr; i += kTileThreads) {
-      const int row = i / kVpr, col = i % kVpr;
-      const uint4 v = *reinterpret_cast<const uint4*>(
-        lin + in0 + uint64_t(row) * a.in_stride[0] + uint64_t(col) * kVec);
-      *reinterpret_cast<uint4*>(cur + row * TE + col * kVec) = v;
-      *reinterpret_cast<uint4*>(slot + out0 + uint64_t(row) * a.lv[0].s[0] +
-                                uint64_t(col) * kVec) = v;
-    }
-  } else
-  for (int i = threadIdx.x; i < TN; i += kTileThreads) {
-    uint32_t x[3], in = 1;
-    int r = i;
+  // Every thread issues all its L0 loads before its first store (the
+  // stores could alias the input as far as the compiler knows, so it would
+  // not hoist the loads itself).
+  if constexpr (D == 2) {
+    if (fast) {
+      constexpr int kVec = 16 / int(sizeof(T)); // elements per vector
+      constexpr int kVpr = TE / kVec;           // vectors per row
+      constexpr int kIt = TE * kVpr / kTileThreads;
+      constexpr int kG = kIt < 4 ? kIt : 4; // vectors in flight per thread
+#pragma unroll 1
+      for (int g = 0; g < kIt; g += kG) {
+        uint4 v[kG];
 #pragma unroll
-    for (int k = D - 1; k >= 0; --k) { // row-major in the tile, last LOD dim fastest
-      x[k] = org[k] + (r & (TE - 1));
-      in &= (r & (TE - 1)) < int(ext[k]);
-      r >>= TL;
-    }
-    if (in) {
-      uint64_t off = 0;
+        for (int s = 0; s < kG; ++s) {
+          const int i = (g + s) * kTileThreads + int(threadIdx.x);
+          const int row = i / kVpr, col = i % kVpr;
+          v[s] = *reinterpret_cast<const uint4*>(
+            lin + in0 + uint64_t(row) * a.in_stride[0] + uint64_t(col) * kVec);
+        }
 #pragma unroll
-      for (int k = 0; k < D; ++k)
-        off += uint64_t(x[k]) * a.in_stride[k];
-      const T v = lin[off];
-      cur[i] = v;
-      slot[fixed0 + chunk_pos<D>(a, 0, x)] = v;
+        for (int s = 0; s < kG; ++s) {
+          const int i = (g + s) * kTileThreads + int(threadIdx.x);
+          const int row = i / kVpr, col = i % kVpr;
+          *reinterpret_cast<uint4*>(cur + row * TE + col * kVec) = v[s];
+          *reinterpret_cast<uint4*>(slot + out0 + uint64_t(row) * a.lv[0].s[0] +
+                                    uint64_t(col) * kVec) = v[s];
+        }
+      }
     }
   }
+  if (!fast) {
+    constexpr int kIt = TN / kTileThreads;
+    constexpr int kG = 4; // elements in flight per thread
+#pragma unroll 1
+    for (int g = 0; g < kIt; g += kG) {
+      T v[kG];
+      uint32_t ok = 0;
+#pragma unroll
+      for (int s = 0; s < kG; ++s) {
+        const int i = (g + s) * kTileThreads + int(threadIdx.x);
+        uint32_t in = 1;
+        uint64_t off = 0;
+        int r = i;
+#pragma unroll
+        for (int k = D - 1; k >= 0; --k) { // row-major in the tile, last LOD dim fastest
+          in &= (r & (TE - 1)) < int(ext[k]);
+          off += uint64_t(org[k] + (r & (TE - 1))) * a.in_stride[k];
+          r >>= TL;
+        }
+        if (in) {
+          v[s] = lin[off];
+          ok |= 1u << s;
+        }
+      }
+#pragma unroll
+      for (int s = 0; s < kG; ++s) {
+        if (!((ok >> s) & 1))
+          continue;
+        const int i = (g + s) * kTileThreads + int(threadIdx.x);
+        uint32_t x[3];
+        int r = i;
+#pragma unroll
+        for (int k = D - 1; k >= 0; --k) {
+          x[k] = org[k] + (r & (TE - 1));
+          r >>= TL;
+        }
+        cur[i] = v[s];
+        slot[fixed0 + chunk_pos<D>(a, 0, x)] = v[s];
+      }
+    }
+  }
+#pragma unroll
+  for (int s = 0; s < kPre; ++s)
+    if ((pre_ok >> s) & 1)
+      stage[s * kTileThreads + int(threadIdx.x)] = pre[s];
   __syncthreads();
 
   // ---- levels 1.. ----
-  int edge = TE, elog = TL;
+  int edge = TE, elog = TL, sbase = 0;
   for (int l = 1; l < a.nlod && l <= TL; ++l) {
     const int pe = edge >> 1; // parent tile edge
     const int plog = elog - 1;
@@ -221,7 +320,8 @@ lod_tile_k(LodTileArgs a)
       if (!inchunk)
         pos = fixedl + chunk_pos<D>(a, l, gx);
       if (fold) {
-        // dense accumulator [fixed][row-major level coords]
+        // dense accumulator [fixed][row-major level coords]; its value
+        // before this epoch is in the stage
         uint64_t ai = 0;
 #pragma unroll
         for (int k = 0; k < D; ++k)
@@ -229,7 +329,8 @@ lod_tile_k(LodTileArgs a)
         T* acc = reinterpret_cast<T*>(a.accum) + a.lv[l].accum_off +
                  b * a.lv[l].nelem + ai;
         const uint32_t cnt = a.count[l];
-        const T av = cnt == 0 ? v : fold_one<T>(*acc, v, l, a.append_method);
+        const T av =
+          cnt == 0 ? v : fold_one<T>(stage[sbase + i], v, l, a.append_method);
         *acc = av;
         if (emit)
           slot[pos] = emit_one<T>(av, cnt + 1, a.append_method);
@@ -249,6 +350,7 @@ lod_tile_k(LodTileArgs a)
     }
     edge = pe;
     elog = plog;
+    sbase += pn;
     __syncthreads();
   }
 }
@@ -285,7 +387,7 @@ cudaError_t launch_tile_typed(const LodTileArgs& a, cudaStream_t st)
     tiles *= a.tiles[k];
   const dim3 grid(unsigned(tiles), unsigned(a.fixed_count));
   const size_t tn = size_t(1) << (D * TL);
-  const size_t smem = sizeof(T) * (tn + (tn >> D));
+  const size_t smem = sizeof(T) * (tn + (tn >> D) + size_t(stage_elems<D>()));
   if (smem > 48 * 1024)
     cudaFuncSetAttribute(lod_tile_k<T, D>,
                          cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
