@@ -27,7 +27,31 @@ __device__ __forceinline__ void copy_bytes(uint8_t* dst,
   const uintptr_t sa = reinterpret_cast<uintptr_t>(s);
   const uint32_t* w = reinterpret_cast<const uint32_t*>(sa & ~uintptr_t(3));
   const unsigned sh = unsigned(sa & 3) * 8;
-  for (uint64_t v = lane; v < nvec; v += lanes) {
+  // kBatch vectors per thread and step: all their loads are issued before
+  // the first store (the compiler may not move a load above a store that
+  // could alias it), so a thread waits on memory once per step
+  constexpr int kBatch = 4;
+  uint64_t v = lane;
+  for (; v + (kBatch - 1) * uint64_t(lanes) < nvec; v += kBatch * uint64_t(lanes)) {
+    uint32_t r[kBatch][5];
+#pragma unroll
+    for (int u = 0; u < kBatch; ++u) {
+      const uint32_t* p = w + 4 * (v + u * uint64_t(lanes));
+#pragma unroll
+      for (int k = 0; k < 5; ++k)
+        r[u][k] = p[k];
+    }
+#pragma unroll
+    for (int u = 0; u < kBatch; ++u) {
+      uint4 o;
+      o.x = __funnelshift_r(r[u][0], r[u][1], sh);
+      o.y = __funnelshift_r(r[u][1], r[u][2], sh);
+      o.z = __funnelshift_r(r[u][2], r[u][3], sh);
+      o.w = __funnelshift_r(r[u][3], r[u][4], sh);
+      d[v + u * uint64_t(lanes)] = o;
+    }
+  }
+  for (; v < nvec; v += lanes) {
     const uint32_t* p = w + 4 * v;
     const uint32_t w0 = p[0], w1 = p[1], w2 = p[2], w3 = p[3], w4 = p[4];
     uint4 o;

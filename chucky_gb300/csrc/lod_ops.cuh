@@ -116,6 +116,85 @@ __device__ T reduce_window(const T* src, uint64_t n, int method)
   return src[0];
 }
 
+// reduce_window for a full window of N values held in registers: the same
+// operations in the same order (sums in window order, the insertion sort
+// of the median with its comparisons in the same sequence), with
+// compile-time indices so that nothing goes through local memory.
+template<typename T, int N>
+__device__ __forceinline__ T reduce_full(T (&w)[N], int method)
+{
+  using A = typename WideAcc<T>::type;
+  switch (method) {
+    case lod_reduce_mean: {
+      A sum = A(0);
+#pragma unroll
+      for (int j = 0; j < N; ++j)
+        sum += to_acc<T>(w[j]);
+      return from_acc<T>(sum / A(N));
+    }
+    case lod_reduce_min: {
+      T v = w[0];
+#pragma unroll
+      for (int j = 1; j < N; ++j)
+        if (lt(w[j], v))
+          v = w[j];
+      return v;
+    }
+    case lod_reduce_max: {
+      T v = w[0];
+#pragma unroll
+      for (int j = 1; j < N; ++j)
+        if (lt(v, w[j]))
+          v = w[j];
+      return v;
+    }
+    case lod_reduce_median: {
+#pragma unroll
+      for (int i = 1; i < N; ++i) {
+        const T key = w[i];
+        bool go = true; // still shifting larger elements up
+#pragma unroll
+        for (int k = i; k > 0; --k) {
+          const bool sh = go && lt(key, w[k - 1]);
+          const T nk = sh ? w[k - 1] : (go ? key : w[k]);
+          go = sh;
+          w[k] = nk;
+        }
+        if (go)
+          w[0] = key;
+      }
+      return w[N / 2];
+    }
+    case lod_reduce_max_suppressed: {
+      T t1 = w[0], t2 = w[0];
+#pragma unroll
+      for (int j = 1; j < N; ++j) {
+        const T v = w[j];
+        if (!lt(v, t1)) { // v >= t1
+          t2 = t1;
+          t1 = v;
+        } else if (lt(t2, v))
+          t2 = v;
+      }
+      return t2;
+    }
+    case lod_reduce_min_suppressed: {
+      T t1 = w[0], t2 = w[0];
+#pragma unroll
+      for (int j = 1; j < N; ++j) {
+        const T v = w[j];
+        if (!lt(t1, v)) { // v <= t1
+          t2 = t1;
+          t1 = v;
+        } else if (lt(v, t2))
+          t2 = v;
+      }
+      return t2;
+    }
+  }
+  return w[0];
+}
+
 // (a + b) >> s without overflow for 8..32-bit integers; a + b otherwise
 // (the dim-0 mean divides at emit for floats; 64-bit ints just sum).
 template<typename T>

@@ -289,22 +289,40 @@ lod_tile_k(LodTileArgs a)
       if (!in)
         continue;
       // children in Z order of the offset (dim 0 = least significant bit)
-      T win[8];
-      int n = 0;
+      bool full = true;
 #pragma unroll
-      for (int z = 0; z < (1 << D); ++z) {
-        int ci = 0;
-        bool ok = true;
+      for (int k = 0; k < D; ++k)
+        full &= 2 * p[k] + 1 < cext[k];
+      T v;
+      if (full) { // every child in bounds: the window stays in registers
+        T w[1 << D];
 #pragma unroll
-        for (int k = 0; k < D; ++k) {
-          const uint32_t c = 2 * p[k] + ((z >> k) & 1);
-          ok &= c < cext[k];
-          ci = (ci << elog) + int(c);
+        for (int z = 0; z < (1 << D); ++z) {
+          int ci = 0;
+#pragma unroll
+          for (int k = 0; k < D; ++k)
+            ci = (ci << elog) + int(2 * p[k] + ((z >> k) & 1));
+          w[z] = cur[ci];
         }
-        if (ok)
-          win[n++] = cur[ci];
+        v = reduce_full<T, (1 << D)>(w, a.method);
+      } else {
+        T win[8];
+        int n = 0;
+#pragma unroll
+        for (int z = 0; z < (1 << D); ++z) {
+          int ci = 0;
+          bool ok = true;
+#pragma unroll
+          for (int k = 0; k < D; ++k) {
+            const uint32_t c = 2 * p[k] + ((z >> k) & 1);
+            ok &= c < cext[k];
+            ci = (ci << elog) + int(c);
+          }
+          if (ok)
+            win[n++] = cur[ci];
+        }
+        v = reduce_window<T>(win, uint64_t(n), a.method);
       }
-      const T v = reduce_window<T>(win, uint64_t(n), a.method);
       int pi = 0;
 #pragma unroll
       for (int k = 0; k < D; ++k)

@@ -9,8 +9,9 @@
 // last match starting >= 12 bytes before the end) in three passes:
 //   find : warp-parallel greedy match finding per 4 KiB segment, matches
 //          reaching back across the 16 KiB region (lz77.cuh)
-//   plan : per chunk, carry each segment's trailing literals into the next
-//          segment's first sequence and place every segment in the output
+//   plan : a warp per chunk carries each segment's trailing literals into
+//          the next segment's first sequence and places every segment in
+//          the output (segmented scans over the segments)
 //   emit : a warp writes its segment's sequences at that place.
 #include "kernels_codec.hpp"
 #include "copy.cuh"
@@ -102,42 +103,100 @@ lz4_find_k(CodecBatch b, Seq* seqs, SegMeta* meta, uint32_t regions_per_chunk)
 // chunk's output.  Trailing literals of a segment (all of it when it has no
 // match) belong to the literal field of the next sequence: the first
 // sequence of a later segment, or the final literal-only sequence.
-__global__ void lz4_plan_k(CodecBatch b, SegMeta* meta)
+//
+// A warp per chunk, 32 segments per step.  Forward pass: the literals
+// carried into each segment are a segmented sum of the trailing counts (a
+// segment with matches restarts the run with its own trailing literals),
+// and the output offsets an exclusive sum of the segments' sizes.  Reverse
+// pass: each segment's trailing literals go to the literal field of the
+// next segment with matches (or of the final sequence), after the run's
+// earlier contributions.
+__global__ void __launch_bounds__(32 * kWarps)
+lz4_plan_k(CodecBatch b, SegMeta* meta)
 {
-  const uint64_t chunk = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x;
+  constexpr unsigned kAll = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const uint64_t chunk = uint64_t(blockIdx.x) * kWarps + (threadIdx.x >> 5);
   if (chunk >= b.n_chunks)
-    return;
+    return; // the whole warp
   SegMeta* m = meta + chunk * b.segs_per_chunk;
-  uint64_t off = 0;
-  uint32_t carry = 0;   // literals of the pending run
-  uint32_t run_first = 0; // first segment contributing to the pending run
-  auto settle = [&](uint64_t field, uint32_t upto) {
-    // the run's literal field starts at `field`; place contributors' tails
-    uint64_t pos = field;
-    for (uint32_t j = run_first; j < upto; ++j) {
-      m[j].tail_dst = pos;
-      pos += m[j].trailing;
+  const uint32_t S = b.segs_per_chunk;
+  uint32_t carry = 0; // literals pending before the group
+  uint64_t off = 0;   // output bytes before the group
+  for (uint32_t g = 0; g < S; g += 32) {
+    const uint32_t k = g + lane;
+    const bool valid = k < S;
+    uint32_t tr = 0, fl = 0, body = 0;
+    bool has = false;
+    if (valid) {
+      has = m[k].nseq != 0;
+      tr = m[k].trailing;
+      fl = m[k].first_lit;
+      body = m[k].body;
     }
-  };
-  for (uint32_t k = 0; k < b.segs_per_chunk; ++k) {
-    m[k].carry_in = carry;
-    m[k].out_off = off;
-    if (m[k].nseq) {
-      const uint32_t ll = m[k].first_lit + carry;
-      settle(off + 1 + ext_len(ll), k);
-      off += lit_part(ll) + m[k].body;
-      carry = m[k].trailing;
-      run_first = k;
-    } else {
-      carry += m[k].trailing;
+    // carry out of segment k, counted from the group start unless a
+    // segment with matches in [g, k] restarted the run
+    uint32_t x = tr;
+    bool f = has;
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t xp = __shfl_up_sync(kAll, x, o);
+      const bool fp = __shfl_up_sync(kAll, f, o);
+      if (lane >= o) {
+        if (!f)
+          x += xp;
+        f = f || fp;
+      }
     }
+    const uint32_t cout = f ? x : carry + x;
+    uint32_t cin = __shfl_up_sync(kAll, cout, 1);
+    if (lane == 0)
+      cin = carry;
+    const uint64_t c = has ? uint64_t(lit_part(fl + cin)) + body : 0;
+    uint64_t inc = c;
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint64_t y = __shfl_up_sync(kAll, inc, o);
+      if (lane >= o)
+        inc += y;
+    }
+    if (valid) {
+      m[k].carry_in = cin;
+      m[k].out_off = off + inc - c;
+    }
+    off += __shfl_sync(kAll, inc, 31);
+    carry = __shfl_sync(kAll, cout, 31); // lanes past S add nothing
   }
-  // final literal-only sequence carries the pending run
-  settle(off + 1 + ext_len(carry), b.segs_per_chunk);
-  m[b.segs_per_chunk - 1].final_off = off;
-  m[b.segs_per_chunk - 1].final_ll = carry;
-  off += lit_part(carry);
-  b.out_sizes[b.id(chunk)] = off;
+  if (lane == 0) {
+    m[S - 1].final_off = off;
+    m[S - 1].final_ll = carry;
+    b.out_sizes[b.id(chunk)] = off + lit_part(carry);
+  }
+  __syncwarp();
+  // literal field of the run that ends at the final sequence
+  uint64_t next_field = off + 1 + ext_len(carry);
+  const uint32_t ngroups = (S + 31) / 32;
+  for (uint32_t gi = ngroups; gi-- > 0;) {
+    const uint32_t k = gi * 32 + lane;
+    const bool valid = k < S;
+    bool has = false;
+    uint64_t field = 0;
+    uint32_t in_run = 0; // place of the segment's tail within its run
+    if (valid) {
+      has = m[k].nseq != 0;
+      const uint32_t cin = m[k].carry_in;
+      if (has)
+        field = m[k].out_off + 1 + ext_len(m[k].first_lit + cin);
+      else
+        in_run = cin;
+    }
+    const unsigned hm = __ballot_sync(kAll, has);
+    const unsigned above = lane == 31 ? 0u : hm & (kAll << (lane + 1));
+    const uint64_t f_above = __shfl_sync(kAll, field, above ? __ffs(int(above)) - 1 : 0);
+    if (valid)
+      m[k].tail_dst = (above ? f_above : next_field) + in_run;
+    const uint64_t f_first = __shfl_sync(kAll, field, hm ? __ffs(int(hm)) - 1 : 0);
+    if (hm)
+      next_field = f_first;
+  }
 }
 
 __device__ __forceinline__ uint8_t* put_len(uint8_t* o, uint32_t extra)
@@ -261,7 +320,8 @@ cudaError_t launch_lz4(CodecBatch b, void* scratch, cudaStream_t st)
                 kRegionStageWords * sizeof(uint32_t), st, b, seqs, meta, rpc);
   if ((e = cudaGetLastError()) != cudaSuccess)
     return e;
-  CHUCKY_LAUNCH(lz4_plan_k, unsigned((b.n_chunks + 127) / 128), 128, 0, st, b, meta);
+  CHUCKY_LAUNCH(lz4_plan_k, unsigned((b.n_chunks + kWarps - 1) / kWarps), 32 * kWarps, 0,
+                st, b, meta);
   if ((e = cudaGetLastError()) != cudaSuccess)
     return e;
   CHUCKY_LAUNCH(lz4_emit_k, grid, 32 * kWarps, 0, st, b, seqs, meta);

@@ -181,7 +181,10 @@ __device__ inline SegInfo lz77_parse_segment(const uint32_t* words,
   auto take = [&](unsigned hits, uint32_t base, uint32_t step, uint32_t cand,
                   uint32_t len) {
     for (;;) {
-      const uint32_t from = p > base ? (p - base + step - 1) / step : 0;
+      // first lane at or after the parse point (no division while the
+      // probing is dense: matches come often then)
+      const uint32_t d = p > base ? p - base : 0;
+      const uint32_t from = step == 1 ? d : (d + step - 1) / step;
       if (from >= 32)
         break;
       const unsigned m = hits & (0xffffffffu << from);

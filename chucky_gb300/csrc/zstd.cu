@@ -1156,9 +1156,18 @@ zstd_block_k(CodecBatch b,
     }
   }
   if (tid == 0) {
+    // the block's segment records, loaded together
+    ZSeg ms[kSegsPerBlock];
+#pragma unroll
+    for (uint32_t k = 0; k < kSegsPerBlock; ++k)
+      if (k < nsegs)
+        ms[k] = meta[segbase + k];
     uint32_t carry = 0, matched_before = 0, nseq = 0;
-    for (uint32_t k = 0; k < nsegs; ++k) {
-      const ZSeg m = meta[segbase + k];
+#pragma unroll
+    for (uint32_t k = 0; k < kSegsPerBlock; ++k) {
+      if (k >= nsegs)
+        break;
+      const ZSeg m = ms[k];
       const uint32_t s0 = b0 + k * kSegBytes;
       S.seg_nseq[k] = m.nseq;
       S.seg_seq0[k] = nseq;
@@ -1173,9 +1182,12 @@ zstd_block_k(CodecBatch b,
     // single-valued input (RLE block) and literals (RLE literals section)
     uint32_t all_same = 1, lit_same = 1;
     int lit_byte = -1;
-    const uint32_t in0 = (meta[segbase].flags >> 16) & 0xFF;
-    for (uint32_t k = 0; k < nsegs; ++k) {
-      const ZSeg m = meta[segbase + k];
+    const uint32_t in0 = (ms[0].flags >> 16) & 0xFF;
+#pragma unroll
+    for (uint32_t k = 0; k < kSegsPerBlock; ++k) {
+      if (k >= nsegs)
+        break;
+      const ZSeg m = ms[k];
       const uint32_t s0 = b0 + k * kSegBytes;
       const uint32_t nl = min(b1, s0 + kSegBytes) - s0 - m.matched;
       all_same &= (m.flags >> 24) & ((m.flags >> 16) & 0xFF) == in0;

@@ -55,7 +55,9 @@ static void fill(uint8_t* p, size_t n, const std::string& pat, size_t chunk)
     else if (pat == "geom") { // skewed: P(k) ~ 2^-(k+1), rare other bytes
       const uint64_t r = rnd();
       p[i] = (r & 511) == 0 ? uint8_t(r >> 9) : uint8_t(__builtin_ctzll(r | (1ull << 40)));
-    } else if (pat == "ramp")
+    } else if (pat == "halves") // random first half of each chunk, zeros after
+      p[i] = (i % chunk) < chunk / 2 ? uint8_t(rnd()) : 0;
+    else if (pat == "ramp")
       p[i] = uint8_t(i % 251);
     else if (pat == "xor16") { // u16 (x^y^z)*257 + noise(0..15)
       const size_t e = i / 2, x = e % 64, y = (e / 64) % 64, z = e / 4096;

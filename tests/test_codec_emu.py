@@ -40,7 +40,10 @@ BIG = [("zstd", "xor16", 200000, 1), ("zstd", "mixed", 131072, 2),
        ("zstd", "geom", 40000, 1), ("lz4", "geom", 9000, 1),
        # FSE-coded Huffman weights (more than 128), both parities of their
        # count (the two interleaved state chains end on either state)
-       ("zstd", "u200", 70000, 1), ("zstd", "u201", 70000, 1)]
+       ("zstd", "u200", 70000, 1), ("zstd", "u201", 70000, 1),
+       # more than 32 segments per chunk, whole groups of 32 segments
+       # without a match before and after ones with matches
+       ("lz4", "halves", 300000, 2), ("lz4", "random", 270000, 1)]
 
 
 def _run(emu, codec, pattern, chunk, n):
