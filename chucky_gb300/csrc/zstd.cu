@@ -904,6 +904,7 @@ zstd_table_k(CodecBatch b,
     const uint32_t fi = T.hist[tid];
     if (fi) {
       int rank = 0;
+#pragma unroll 16
       for (int j = 0; j < 256; ++j) {
         const uint32_t fj = T.hist[j];
         rank += fj && (fj < fi || (fj == fi && j < tid));
@@ -997,19 +998,35 @@ zstd_table_k(CodecBatch b,
       // (as zlib's gen_bitlen repairs its length counts): one unit less.
       uint32_t* bl = x.count_w;
       constexpr int M = int(kHufMaxBits);
+      // the counts stay in registers through the repair (every index
+      // below is a compile-time constant after unrolling)
+      uint32_t r[M + 1];
+#pragma unroll
+      for (int L = 0; L <= M; ++L)
+        r[L] = bl[L];
       uint32_t units = 0;
+#pragma unroll
       for (int L = 1; L <= M; ++L)
-        units += bl[L] << (M - L);
+        units += r[L] << (M - L);
       for (uint32_t excess = units - (1u << M); int(excess) > 0; --excess) {
-        int bits = M - 1;
-        while (bits > 0 && bl[bits] == 0)
-          --bits;
-        if (bits == 0 || bl[M] == 0)
+        int bits = 0; // the deepest level above the limit with a leaf
+#pragma unroll
+        for (int L = 1; L < M; ++L)
+          if (r[L])
+            bits = L;
+        if (bits == 0 || r[M] == 0)
           break;
-        bl[bits]--;
-        bl[bits + 1] += 2;
-        bl[M]--;
+#pragma unroll
+        for (int L = 1; L < M; ++L)
+          if (L == bits) {
+            r[L]--;
+            r[L + 1] += 2;
+          }
+        r[M]--;
       }
+#pragma unroll
+      for (int L = 0; L <= M; ++L)
+        bl[L] = r[L];
       int mb = 0;
       uint32_t kraft = 0;
       for (int L = 1; L <= int(kHufMaxBits); ++L)
@@ -1076,8 +1093,15 @@ zstd_table_k(CodecBatch b,
     if (tid == 0)
       T.bits = 0;
     __syncthreads();
-    if (T.ok && sym < 256 && len > 0)
-      atomicAdd(&T.bits, (unsigned long long)T.hist[sym] * uint32_t(len));
+    {
+      // one shared atomic per warp: 256 on one address serialise
+      unsigned long long cb =
+        T.ok && sym < 256 && len > 0 ? (unsigned long long)T.hist[sym] * uint32_t(len) : 0;
+      for (int o = 16; o; o >>= 1)
+        cb += __shfl_xor_sync(0xffffffffu, cb, o);
+      if (lane == 0 && cb)
+        atomicAdd(&T.bits, cb);
+    }
     __syncthreads();
     if (tid == 0 && T.ok)
       T.ok = T.bits / 8 + uint32_t(h.desc_len) + 16 < uint64_t(T.total);
