@@ -353,8 +353,8 @@ def run_ours(args, rank, world):
     per_launch_ms = comp_ms / max(1, comp_launches)
     per_launch_bytes = comp_in / max(1, comp_launches)
     # DRAM bytes (read + written) per byte of encoder input, measured by ncu
-    # on one batch of the u16 cube: 55.1 MB for 19.40 MB of chunk input
-    traffic_per_input_byte = 2.84 if args.workload == "multiscale" else None
+    # on one batch of the u16 cube: 54.9 MB for 19.40 MB of chunk input
+    traffic_per_input_byte = 2.83 if args.workload == "multiscale" else None
     peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     peak, peak_src = 6800.0, "fallback"
     if os.path.exists(peaks_path):
