@@ -129,6 +129,65 @@ def cube_lz4_config():
     return cfg
 
 
+# rank-5 (t, c, z, y, x) arrays of 3 x 128 x 512 x 512 per time point,
+# t scaled per dtype so that every array holds 768 MiB
+BATCHED_DTYPES = (("u8", 8, "max_sup"), ("i16", 4, "min_sup"), ("u16", 4, "max_sup"),
+                  ("f16", 4, "min_sup"), ("f32", 2, "max_sup"))
+
+
+def batched_config(dtype, t, reduce):
+    """Chunk 1x1x32x128x128, shard 1x1x4x4x4 chunks, (z, y, x) pyramid
+    (4 levels asked; the level rule of the planner gives 3), zstd-1."""
+    dims = capi.make_dims([
+        dict(size=t, chunk=1, cps=1, name="t"),
+        dict(size=3, chunk=1, cps=1, name="c"),
+        dict(size=128, chunk=32, cps=4, downsample=1, name="z"),
+        dict(size=512, chunk=128, cps=4, downsample=1, name="y"),
+        dict(size=512, chunk=128, cps=4, downsample=1, name="x")])
+    cfg = capi.make_config(dims, dtype=dtype, codec="zstd", level=1, reduce=reduce,
+                           append_reduce=reduce, max_nlod=4,
+                           epochs_per_batch=EPOCHS_PER_BATCH,
+                           buffer_capacity_bytes=128 << 20)
+    cfg._dims = dims
+    return cfg
+
+
+def batched_array(dtype, t, dev, seed=13):
+    """Chunk classes by a seeded hash of the chunk index: half all-zero, a
+    quarter one constant value, a quarter uniform random (compressed sizes
+    spread over more than 100x).  Returns the device tensor."""
+    import torch
+    tdt = {"u8": torch.uint8, "i16": torch.int16, "u16": torch.int16,
+           "f16": torch.float16, "f32": torch.float32}[dtype]
+    out = torch.zeros((t, 3, 128, 512, 512), dtype=tdt, device=dev)
+    g = torch.Generator(device=dev)
+    g.manual_seed(seed)
+    rng = np.random.default_rng(seed)
+    for ti in range(t):
+        for ci in range(3):
+            for cz in range(4):
+                for cy in range(4):
+                    for cx in range(4):
+                        u = rng.random()
+                        if u < 0.5:
+                            continue
+                        view = out[ti, ci, cz * 32:(cz + 1) * 32, cy * 128:(cy + 1) * 128,
+                                   cx * 128:(cx + 1) * 128]
+                        if u < 0.75:
+                            view.fill_(int(rng.integers(1, 100)))
+                        elif tdt.is_floating_point:
+                            view.copy_(torch.rand(view.shape, generator=g, device=dev,
+                                                  dtype=torch.float32).to(tdt))
+                        else:
+                            bits = 8 if tdt == torch.uint8 else 16
+                            r = torch.randint(0, 1 << bits, view.shape, generator=g,
+                                              device=dev, dtype=torch.int32)
+                            if bits == 16:
+                                r = r - (1 << 15)
+                            view.copy_(r.to(tdt))
+    return out
+
+
 def make_workload(name, dev, frames):
     """(description, data note, dtype, [(config, pinned host bytes, device
     bytes)], encoder name) of a workload."""
@@ -167,6 +226,19 @@ def make_workload(name, dev, frames):
         return (desc, "synthetic (seeded Poisson(100) + 64 Gaussian blobs, 12-bit; "
                 "generated on the device)", "u16",
                 [(sensor_config(codec, "max"), host, dbuf)], enc)
+    if name == "batched":
+        arrays = []
+        for dt, t, red in BATCHED_DTYPES:
+            host, dbuf = pair(batched_array(dt, t, dev))
+            arrays.append((batched_config(dt, t, red), host, dbuf))
+        desc = ("5 rank-5 (t,c,z,y,x) arrays t x 3 x 128 x 512 x 512, one per dtype "
+                "(u8 t=8, i16 t=4, u16 t=4, f16 t=4, f32 t=2: 768 MiB each), chunk "
+                "1x1x32x128x128, shard 1x1x4x4x4 chunks, (z,y,x) max_sup/min_sup pyramid "
+                "(3 levels), half the chunks zero, a quarter constant, a quarter random, "
+                "zstd-1, K=%d epochs per batch, one host thread per array, discard sink"
+                % EPOCHS_PER_BATCH)
+        return (desc, "synthetic (seeded chunk classes: zero / constant / uniform random)",
+                "u8+i16+u16+f16+f32", arrays, "zstd encoder (find+table+block+frame)")
     raise ValueError(name)
 
 
@@ -535,10 +607,12 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     ap.add_argument("--workload", default="multiscale",
-                    choices=["multiscale", "cube-lz4", "sensor-zstd", "sensor-lz4"],
+                    choices=["multiscale", "cube-lz4", "sensor-zstd", "sensor-lz4",
+                             "batched"],
                     help="multiscale: the plain multiscale line (default); cube-lz4: "
                          "the 256^3 u16 cube with LZ4 and no LOD; sensor-*: 2304x4096 "
-                         "u16 frames with a 5-level dim-0 pyramid")
+                         "u16 frames with a 5-level dim-0 pyramid; batched: five rank-5 "
+                         "arrays of different dtypes with uneven chunk classes")
     ap.add_argument("--frames", type=int, default=512,
                     help="sensor frames per step (multiple of 32)")
     ap.add_argument("--single", choices=["u16", "f32", "cube-lz4", "sensor-zstd",
