@@ -177,39 +177,83 @@ __device__ inline SegInfo lz77_parse_segment(const uint32_t* words,
   }
   __syncwarp();
   uint32_t w0 = first, p = first, lit_start = first, nseq = 0;
-  // greedy parse of one window's hits (lanes at or after the parse point)
+  // Greedy parse of one window's hits (lanes at or after the parse point).
+  // Every hit lane knows where its match ends, hence the first hit lane at
+  // or after that end: the greedy choices are the chain of these links from
+  // the first hit lane at or after p, walked with one shuffle per match,
+  // and the chosen lanes then write their sequences side by side.  A match
+  // measured to kLaneExtend bytes ends the chain; the warp extends it and
+  // the parse continues after its true end.
+  const unsigned below_me = (1u << lane) - 1;
   auto take = [&](unsigned hits, uint32_t base, uint32_t step, uint32_t cand,
                   uint32_t len) {
+    const uint32_t mpos_l = base + lane * step;
+    const uint32_t end_l = mpos_l + len;
+    const unsigned longs = __ballot_sync(0xffffffffu, ((hits >> lane) & 1) && len >= kLaneExtend);
+    // first lane at or after position x (no division while the probing is
+    // dense: matches come often then)
+    auto lane_from = [&](uint32_t x) {
+      const uint32_t d = x > base ? x - base : 0;
+      return step == 1 ? d : (d + step - 1) / step;
+    };
+    int nxt = 32; // next hit lane after this lane's match
+    if ((hits >> lane) & 1) {
+      const uint32_t f = lane_from(end_l);
+      const unsigned nm = f >= 32 ? 0u : hits & (0xffffffffu << f);
+      nxt = nm ? __ffs(int(nm)) - 1 : 32;
+    }
     for (;;) {
-      // first lane at or after the parse point (no division while the
-      // probing is dense: matches come often then)
-      const uint32_t d = p > base ? p - base : 0;
-      const uint32_t from = step == 1 ? d : (d + step - 1) / step;
+      const uint32_t from = lane_from(p);
       if (from >= 32)
         break;
       const unsigned m = hits & (0xffffffffu << from);
       if (!m)
         break;
-      const int k = __ffs(int(m)) - 1;
-      const uint32_t mpos = base + k * step;
-      const uint32_t src = __shfl_sync(0xffffffffu, cand, k);
-      uint32_t mlen = __shfl_sync(0xffffffffu, len, k);
-      if (mlen >= kLaneExtend) { // long match: the warp extends it
-        for (;;) {
-          const uint32_t a = mpos + mlen + lane, b = src + mlen + lane;
-          const bool same = a < end && bytes[a] == bytes[b];
-          const unsigned eq = __ballot_sync(0xffffffffu, same);
-          if (eq == 0xffffffffu) {
-            mlen += 32;
-            continue;
-          }
-          mlen += __ffs(int(~eq)) - 1;
+      unsigned sel = 0;
+      int k = __ffs(int(m)) - 1, last = k;
+      for (;;) {
+        sel |= 1u << k;
+        last = k;
+        if ((longs >> k) & 1)
           break;
+        const int nk = __shfl_sync(0xffffffffu, nxt, k);
+        if (nk >= 32)
+          break;
+        k = nk;
+      }
+      // the literals before a chosen match start at the previous chosen
+      // match's end (the parse point for the first)
+      const unsigned prev = sel & below_me;
+      const int pl = prev ? 31 - __clz(int(prev)) : 0;
+      const uint32_t pend = __shfl_sync(0xffffffffu, end_l, pl);
+      const uint32_t lit0 = prev ? pend : lit_start;
+      const bool extend = (longs >> last) & 1;
+      if (((sel >> lane) & 1) && !(extend && lane == last))
+        out[nseq + __popc(prev)] = Seq{ mpos_l - lit0, len, mpos_l - cand };
+      nseq += __popc(sel);
+      if (!extend) {
+        p = __shfl_sync(0xffffffffu, end_l, last);
+        lit_start = p;
+        break; // the chain ended: no hit starts at or after p
+      }
+      // long match: the warp extends it
+      const uint32_t mpos = base + uint32_t(last) * step;
+      const uint32_t src = __shfl_sync(0xffffffffu, cand, last);
+      const uint32_t ls = __shfl_sync(0xffffffffu, lit0, last);
+      uint32_t mlen = __shfl_sync(0xffffffffu, len, last);
+      for (;;) {
+        const uint32_t a = mpos + mlen + lane, b = src + mlen + lane;
+        const bool same = a < end && bytes[a] == bytes[b];
+        const unsigned eq = __ballot_sync(0xffffffffu, same);
+        if (eq == 0xffffffffu) {
+          mlen += 32;
+          continue;
         }
+        mlen += __ffs(int(~eq)) - 1;
+        break;
       }
       if (lane == 0)
-        out[nseq] = Seq{ mpos - lit_start, mlen, mpos - src };
-      ++nseq;
+        out[nseq - 1] = Seq{ mpos - ls, mlen, mpos - src };
       p = mpos + mlen;
       lit_start = p;
     }
