@@ -19,7 +19,8 @@
 // up to kLaneExtend bytes; then all 32 positions enter the table.  The
 // greedy parse then takes, within the window, the lowest position at or
 // after the parse point with a match of at least `min_match` bytes, as many
-// times as the window allows; a match that reaches kLaneExtend bytes is
+// times as the window allows (a chain walk over per-lane links to the next
+// hit after each match); a match that reaches kLaneExtend bytes is
 // extended by the whole warp, 32 bytes per step.  Windows inside a long
 // match are skipped.  Matches end inside their segment and start inside
 // it or its history.  (When lanes of one window share a hash slot the

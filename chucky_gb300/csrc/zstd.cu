@@ -925,9 +925,11 @@ zstd_table_k(CodecBatch b,
   if (build && tid == 0) {
     uint32_t* f = x.f;
     int16_t* parent = x.parent;
-    // the heads of both queues stay in registers (empty: ~0u)
+    // The first two entries of both queues stay in registers (empty: ~0u),
+    // so taking an entry never waits for a shared-memory load: the entry
+    // after the new head is loaded then and needed one take later.
     int leaf = 0, inode = n, next = n;
-    uint32_t fl = f[0], fi = ~0u;
+    uint32_t fl = f[0], fl2 = n > 1 ? f[1] : ~0u, fi = ~0u, fi2 = ~0u;
     for (int k = 0; k < n - 1; ++k) {
       int pick[2];
       uint32_t val[2];
@@ -936,12 +938,14 @@ zstd_table_k(CodecBatch b,
           pick[t] = leaf;
           val[t] = fl;
           ++leaf;
-          fl = leaf < n ? f[leaf] : ~0u;
+          fl = fl2;
+          fl2 = leaf + 1 < n ? f[leaf + 1] : ~0u;
         } else {
           pick[t] = inode;
           val[t] = fi;
           ++inode;
-          fi = inode < next ? f[inode] : ~0u;
+          fi = fi2;
+          fi2 = inode + 1 < next ? f[inode + 1] : ~0u;
         }
       }
       const uint32_t sum = val[0] + val[1];
@@ -949,6 +953,8 @@ zstd_table_k(CodecBatch b,
       parent[pick[0]] = parent[pick[1]] = int16_t(next);
       if (inode == next) // the internal queue was empty: this node heads it
         fi = sum;
+      else if (inode + 1 == next) // it is the queue's second entry
+        fi2 = sum;
       ++next;
     }
     parent[2 * n - 2] = int16_t(2 * n - 2); // the root is its own parent
