@@ -55,7 +55,7 @@ struct SegMeta
 __global__ void __launch_bounds__(32 * kSegsPerRegion)
 lz4_find_k(CodecBatch b, Seq* seqs, SegMeta* meta, uint32_t regions_per_chunk)
 {
-  __shared__ uint16_t tables[kSegsPerRegion][1 << kHashLog];
+  __shared__ __align__(16) uint16_t tables[kSegsPerRegion][1 << kHashLog];
   CHUCKY_DYN_SHARED(uint32_t, words); // kRegionStageWords
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint64_t chunk = blockIdx.x / regions_per_chunk;

@@ -147,7 +147,8 @@ __device__ __forceinline__ uint32_t lane_match(const uint32_t* words,
 // Parse segment [s0, s1) of a chunk whose bytes from r0 (the region start,
 // r0 <= s0) on are staged in `words`.  Matches may start at positions in
 // [s0, start_limit), reach back to r0 and end at or before `match_end`.
-// `table` holds 1 << kHashLog u16 entries private to this warp.
+// `table` holds 1 << kHashLog u16 entries private to this warp (16-byte
+// aligned).
 __device__ inline SegInfo lz77_parse_segment(const uint32_t* words,
                                              uint32_t r0,
                                              uint32_t s0,
@@ -160,8 +161,10 @@ __device__ inline SegInfo lz77_parse_segment(const uint32_t* words,
 {
   const int lane = threadIdx.x & 31;
   const uint8_t* bytes = reinterpret_cast<const uint8_t*>(words);
-  for (int i = lane; i < (1 << kHashLog); i += 32)
-    table[i] = 0xFFFF;
+  // empty table (16-byte stores: the tables are 16-byte aligned rows)
+  for (int i = lane; i < (1 << kHashLog) / 8; i += 32)
+    reinterpret_cast<uint4*>(table)[i] =
+      make_uint4(0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu, 0xFFFFFFFFu);
   __syncwarp();
   // positions below are relative to r0
   const uint32_t first = s0 - r0;

@@ -193,7 +193,7 @@ zstd_find_k(CodecBatch b,
             uint8_t* litbuf,
             uint32_t regions_per_chunk)
 {
-  __shared__ uint16_t tables[kSegsPerRegion][1 << kHashLog];
+  __shared__ __align__(16) uint16_t tables[kSegsPerRegion][1 << kHashLog];
   CHUCKY_DYN_SHARED(uint32_t, words); // kRegionStageWords
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint64_t chunk = blockIdx.x / regions_per_chunk;
@@ -230,12 +230,16 @@ zstd_find_k(CodecBatch b,
     const uint8_t in0 = sb[0];
     const uint32_t pat = in0 * 0x01010101u;
     const uint32_t* sw = words + (s0 - r0) / 4;
+    // (without matches the literals are the input: the literal pass below
+    // answers it)
     bool same = true;
-    for (uint32_t i = lane; i < n / 4; i += 32)
-      same &= sw[i] == pat;
-    for (uint32_t i = n / 4 * 4 + lane; i < n; i += 32)
-      same &= sb[i] == in0;
-    const bool in_same = __all_sync(0xffffffffu, same);
+    if (info.nseq) {
+      for (uint32_t i = lane; i < n / 4; i += 32)
+        same &= sw[i] == pat;
+      for (uint32_t i = n / 4 * 4 + lane; i < n; i += 32)
+        same &= sb[i] == in0;
+    }
+    bool in_same = __all_sync(0xffffffffu, same);
     // literals: compacted in place, counted, copied out
     const uint32_t nlit =
       lz77_compact_literals(words, r0, s0, s1, out, info.nseq, bitmap);
@@ -267,6 +271,8 @@ zstd_find_k(CodecBatch b,
         atomicAdd(hist + ((v >> (8 * k)) & 255), 1u);
     }
     const bool lit_same = __all_sync(0xffffffffu, same);
+    if (!info.nseq)
+      in_same = lit_same;
     const uint4* src = reinterpret_cast<const uint4*>(sb);
     uint4* dst = reinterpret_cast<uint4*>(litbuf + seg * kSegBytes);
     for (uint32_t i = lane; i < (nlit + 15) / 16; i += 32)

@@ -32,6 +32,7 @@
 #define __launch_bounds__(...)
 #define __restrict__
 #define __grid_constant__
+#define __align__(n) __attribute__((aligned(n)))
 
 typedef int cudaError_t;
 typedef void* cudaStream_t;
