@@ -80,6 +80,31 @@ extern "C"
                                       uint64_t* d_sizes,
                                       void* cuda_stream);
 
+  /* Decode raw LZ4 blocks (CODEC_LZ4_NON_STANDARD chunks) on the device,
+   * for on-device verification and readback; no counterpart in the
+   * reference, which decodes with LZ4_decompress_safe on the host
+   * (src/cpu/compress.c:85).
+   *
+   * Block i is d_in_sizes[i] bytes at d_in + d_in_offsets[i] and decodes
+   * to exactly `chunk_bytes` bytes at d_out + i * out_stride.  All
+   * pointers are device memory.  d_status[i] is set to 0 when block i
+   * decoded to exactly chunk_bytes bytes, 1 when it ends inside a
+   * sequence, 2 for a match offset of 0 or before the chunk start, 3 when
+   * it would write past chunk_bytes, 4 when it ends short of chunk_bytes;
+   * a malformed block is never read or written out of bounds.  Runs
+   * asynchronously on `cuda_stream` (a cudaStream_t; NULL for the default
+   * stream).  Returns 0 when launched, 1 for invalid arguments, 3 for a
+   * CUDA error. */
+  int chucky_lz4_decode_chunks(const void* d_in,
+                               const uint64_t* d_in_offsets,
+                               const uint64_t* d_in_sizes,
+                               size_t n_chunks,
+                               void* d_out,
+                               size_t out_stride,
+                               size_t chunk_bytes,
+                               uint32_t* d_status,
+                               void* cuda_stream);
+
 #ifdef __cplusplus
 }
 #endif

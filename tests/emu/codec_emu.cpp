@@ -7,6 +7,7 @@
 #include "simt.hpp"
 
 #include "../../chucky_gb300/csrc/lz4.cu"
+#include "../../chucky_gb300/csrc/lz4_decode.cu"
 #include "../../chucky_gb300/csrc/zstd.cu"
 
 #include <dlfcn.h>
@@ -163,6 +164,47 @@ int main(int argc, char** argv)
       return 1;
     }
     comp += sizes[c];
+  }
+  if (codec == "lz4") {
+    // the device decoder on the same blocks: every chunk back exactly
+    std::vector<uint64_t> offs(n), lens(n);
+    for (uint64_t c = 0; c < n; ++c) {
+      offs[c] = c * out_stride;
+      lens[c] = sizes[c];
+    }
+    std::vector<uint8_t> back(n * in_stride, 0xAB);
+    std::vector<uint32_t> st(n, 99);
+    if (launch_lz4_decode(out.data(), offs.data(), lens.data(), n, back.data(), in_stride,
+                          chunk, st.data(), nullptr) != cudaSuccess)
+      return 1;
+    for (uint64_t c = 0; c < n; ++c)
+      if (st[c] != 0 || std::memcmp(back.data() + c * in_stride, flat.data() + c * chunk, chunk)) {
+        std::fprintf(stderr, "chunk %llu: device decoder status %u or bytes differ\n",
+                     (unsigned long long)c, st[c]);
+        return 1;
+      }
+    // malformed blocks (cut short, garbage) report an error and stay in
+    // bounds (AddressSanitizer watches every access)
+    std::vector<uint8_t> junk(out_stride * 2);
+    for (auto& x : junk)
+      x = uint8_t(rnd());
+    const uint64_t cut = sizes[0] > 1 ? sizes[0] - 1 : 0;
+    std::vector<uint8_t> bad(cut + 1);
+    std::memcpy(bad.data(), out.data(), cut);
+    const uint8_t* blocks[3] = { bad.data(), junk.data(), junk.data() + 7 };
+    const uint64_t blens[3] = { cut, out_stride, out_stride - 7 };
+    for (int t = 0; t < 3; ++t) {
+      uint64_t o = 0, l = blens[t];
+      uint32_t s = 99;
+      std::vector<uint8_t> tmp(chunk);
+      if (launch_lz4_decode(blocks[t], &o, &l, 1, tmp.data(), chunk, chunk, &s, nullptr) !=
+          cudaSuccess)
+        return 1;
+      if (s == 0 && !(t == 0 && cut == sizes[0])) {
+        std::fprintf(stderr, "malformed block %d decoded as valid\n", t);
+        return 1;
+      }
+    }
   }
   std::printf("ok %s chunk=%u n=%llu pattern=%s ratio=%.3f\n", codec.c_str(), chunk,
               (unsigned long long)n, pat.c_str(), double(n * chunk) / double(comp));
