@@ -53,10 +53,13 @@ def make_cubes(seed=7):
     return u16, f32
 
 
-# two batches of two 64-slice epochs per array and step: the encoders of
-# the first batch overlap the LOD of the second, its copy to the host the
-# second's encoders
-EPOCHS_PER_BATCH = int(os.environ.get("CHUCKY_BENCH_EPOCHS_PER_BATCH", "2"))
+# Epochs per batch.  The cubes go one 64-slice epoch per batch (four
+# batches per array and step: each batch's encoders overlap the next one's
+# LOD, its copy to the host the next one's encoders; measured faster than
+# two or four epochs per batch); the larger workloads two.
+_K_ENV = os.environ.get("CHUCKY_BENCH_EPOCHS_PER_BATCH")
+CUBE_EPOCHS_PER_BATCH = int(_K_ENV or "1")
+EPOCHS_PER_BATCH = int(_K_ENV or "2")
 
 
 def make_config(dtype, reduce):
@@ -64,7 +67,7 @@ def make_config(dtype, reduce):
                            for n in "zyx"])
     cfg = capi.make_config(dims, dtype=dtype, codec="zstd", level=3, reduce=reduce,
                            append_reduce="mean", max_nlod=4,
-                           epochs_per_batch=EPOCHS_PER_BATCH,
+                           epochs_per_batch=CUBE_EPOCHS_PER_BATCH,
                            buffer_capacity_bytes=128 << 20)
     cfg._dims = dims
     return cfg
@@ -72,7 +75,8 @@ def make_config(dtype, reduce):
 
 WORKLOAD = ("256^3 u16 (mean LOD) + 256^3 f32 (median LOD), chunk 64^3, shard "
             "4^3 chunks, 2x2x2 pyramid (3 levels), zstd-3, K=%d epochs per batch "
-            "(%d batches per array), discard sink" % (EPOCHS_PER_BATCH, 4 // EPOCHS_PER_BATCH))
+            "(%d batches per array), discard sink"
+            % (CUBE_EPOCHS_PER_BATCH, 4 // CUBE_EPOCHS_PER_BATCH))
 
 # Further workloads (`--workload`), each printing its own line; the default
 # line is the plain multiscale one above.
@@ -123,7 +127,7 @@ def sensor_config(codec, reduce):
 def cube_lz4_config():
     dims = capi.make_dims([dict(size=SIDE, chunk=CHUNK, cps=4, name=n) for n in "zyx"])
     cfg = capi.make_config(dims, dtype="u16", codec="lz4", level=1,
-                           epochs_per_batch=EPOCHS_PER_BATCH,
+                           epochs_per_batch=CUBE_EPOCHS_PER_BATCH,
                            buffer_capacity_bytes=128 << 20)
     cfg._dims = dims
     return cfg
@@ -211,7 +215,7 @@ def make_workload(name, dev, frames):
         u16, _ = make_cubes()
         host = torch.from_numpy(u16.reshape(-1).view(np.uint8)).pin_memory()
         desc = ("256^3 u16, chunk 64^3, shard 4^3 chunks (one shard), no LOD, LZ4, "
-                "K=%d epochs per batch, discard sink" % EPOCHS_PER_BATCH)
+                "K=%d epochs per batch, discard sink" % CUBE_EPOCHS_PER_BATCH)
         return (desc, "synthetic (seeded xor+noise u16 cube)", "u16",
                 [(cube_lz4_config(), host, host.to(dev))], "lz4 encoder (find+plan+emit)")
     if name in ("sensor-zstd", "sensor-lz4"):
