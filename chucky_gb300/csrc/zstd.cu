@@ -348,7 +348,8 @@ __device__ void norm_weights(const uint32_t* hist, int nsym, int al, int16_t* no
   for (int s = 0; s < nsym; ++s) {
     int c = 0;
     if (hist[s]) {
-      c = int((uint64_t(hist[s]) * size + total / 2) / total);
+      // weight counts (<= 256) times the table size (<= 64): 32 bits do
+      c = int((hist[s] * uint32_t(size) + total / 2) / total);
       c = c < 1 ? 1 : (c > half ? half : c);
     }
     norm[s] = int16_t(c);
@@ -505,7 +506,7 @@ __device__ __forceinline__ bool block_uses_table(bool table_ok, uint32_t nlit, b
 
 struct TableShared
 {
-  uint32_t hist[256];
+  alignas(16) uint32_t hist[256];
   uint16_t sorted[256]; // used symbols by (count, symbol)
   uint32_t nsym, total;
   uint32_t ok;
@@ -909,11 +910,19 @@ zstd_table_k(CodecBatch b,
   if (tid < 256) {
     const uint32_t fi = T.hist[tid];
     if (fi) {
+      // four counts per shared load
       int rank = 0;
-#pragma unroll 16
-      for (int j = 0; j < 256; ++j) {
-        const uint32_t fj = T.hist[j];
-        rank += fj && (fj < fi || (fj == fi && j < tid));
+      const uint4* h4 = reinterpret_cast<const uint4*>(T.hist);
+#pragma unroll 8
+      for (int q = 0; q < 64; ++q) {
+        const uint4 v = h4[q];
+        const uint32_t fv[4] = { v.x, v.y, v.z, v.w };
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const uint32_t fj = fv[u];
+          const int j = 4 * q + u;
+          rank += fj && (fj < fi || (fj == fi && j < tid));
+        }
       }
       T.sorted[rank] = uint16_t(tid);
       atomicAdd(&T.nsym, 1u);
