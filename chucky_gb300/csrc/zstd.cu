@@ -819,14 +819,24 @@ __device__ void huff_describe(TableShared& T, int tid)
     const FseEnc& t = T.tw;
     const int par = tid; // 0: even steps, 1: odd steps
     uint32_t v = fse_init(t, w[nw - 1 - par]);
-    for (int k = par, idx = nw - 3 - par; idx >= 0; k += 2, idx -= 2) {
-      const int s = w[idx];
-      const int cnt = t.count[s];
+    // the next step's weight, count and first state are loaded a step
+    // ahead (they do not depend on the state), so each step waits on one
+    // shared-memory load: the state transition
+    int idx = nw - 3 - par;
+    int s_n = idx >= 0 ? w[idx] : 0;
+    int cnt_n = t.count[s_n], first_n = t.first[s_n];
+    for (int k = par; idx >= 0; k += 2, idx -= 2) {
+      const int cnt = cnt_n, first = first_n;
+      if (idx >= 2) {
+        s_n = w[idx - 2];
+        cnt_n = t.count[s_n];
+        first_n = t.first[s_n];
+      }
       int nb = al - highbit(uint32_t(cnt));
       if ((v >> nb) < uint32_t(cnt))
         --nb;
       c.enc[k] = uint16_t((v & ((1u << nb) - 1)) | (uint32_t(nb) << 8));
-      v = t.states[t.first[s] + ((v >> nb) - cnt)] + (1u << al);
+      v = t.states[first + ((v >> nb) - cnt)] + (1u << al);
     }
     const bool state1 = (nw & 1) ? par == 0 : par == 1;
     if (state1)
