@@ -40,6 +40,7 @@ int Stream::codec_init()
 int Stream::codec_compress(const uint8_t* pool,
                            uint64_t nchunks,
                            const uint32_t* d_ids,
+                           const ChunkRuns* runs,
                            uint8_t* out,
                            uint64_t* sizes,
                            void* scratch,
@@ -60,6 +61,16 @@ int Stream::codec_compress(const uint8_t* pool,
       b.out = out;
       b.out_sizes = sizes;
       b.chunk_ids = d_ids + first;
+    } else if (runs) { // chunk slots as runs
+      b.in = pool;
+      b.out = out;
+      b.out_sizes = sizes;
+      b.n_runs = runs->n;
+      b.id_base = first;
+      for (uint32_t r = 0; r <= runs->n; ++r)
+        b.run_first[r] = runs->first[r];
+      for (uint32_t r = 0; r < runs->n; ++r)
+        b.run_slot[r] = runs->slot[r];
     } else { // slots first .. first + n - 1
       b.in = pool + first * b.in_stride;
       b.out = out + first * comp_stride;

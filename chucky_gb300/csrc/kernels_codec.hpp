@@ -35,12 +35,38 @@ struct CodecBatch
   uint32_t segs_per_chunk;
   int level;
   const uint32_t* chunk_ids; // optional: encode only these chunk slots
+  // Otherwise, optionally, the slots as runs of consecutive slots (a batch
+  // whose levels are not all active): entry id_base + i lies in run r when
+  // run_first[r] <= id_base + i < run_first[r + 1] and is slot
+  // run_slot[r] + (id_base + i - run_first[r]).  Passed by value, so no
+  // table has to reach the device first.
+  static constexpr int kMaxRuns = 16;
+  uint32_t n_runs;
+  uint64_t id_base;
+  uint32_t run_first[kMaxRuns + 1];
+  uint32_t run_slot[kMaxRuns];
 
   // slot of the i-th chunk of the batch
   __host__ __device__ uint64_t id(uint64_t i) const
   {
-    return chunk_ids ? chunk_ids[i] : i;
+    if (chunk_ids)
+      return chunk_ids[i];
+    if (!n_runs)
+      return i;
+    const uint64_t g = id_base + i;
+    uint32_t r = 0;
+    while (r + 1 < n_runs && g >= run_first[r + 1])
+      ++r;
+    return run_slot[r] + (g - run_first[r]);
   }
+};
+
+// The runs of consecutive chunk slots of a batch (see CodecBatch).
+struct ChunkRuns
+{
+  uint32_t n;
+  uint32_t first[CodecBatch::kMaxRuns + 1];
+  uint32_t slot[CodecBatch::kMaxRuns];
 };
 
 size_t lz4_scratch_bytes(uint64_t n_chunks, uint32_t chunk_bytes);

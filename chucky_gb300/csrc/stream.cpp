@@ -660,27 +660,47 @@ int Stream::kick_batch(uint32_t n_epochs, const uint32_t* epoch_masks)
     // the encoders start once this batch's pool half is filled
     CK(cudaEventRecord(ev_pool_ready, s_comp));
     CK(cudaStreamWaitEvent(se, ev_pool_ready, 0));
-    // encode only the chunks of active (epoch, level) pairs
+    // encode only the chunks of active (epoch, level) pairs: runs of
+    // consecutive slots, passed to the encoders by value; a list on the
+    // device only for batches with more runs than that holds
     uint32_t* ids = h_chunk_ids[si];
+    ChunkRuns runs{};
+    bool fits = true;
     uint64_t n = 0;
     for (uint32_t e = 0; e < n_epochs; ++e)
       for (int l = 0; l < P.nlod; ++l)
         if (epoch_masks[e] >> l & 1) {
           const uint64_t base = uint64_t(e) * P.total_chunks + P.lv[l].chunk_offset;
-          for (uint64_t j = 0; j < P.lv[l].layout.chunks_per_epoch; ++j)
+          const uint64_t cnt = P.lv[l].layout.chunks_per_epoch;
+          if (runs.n > 0 && runs.slot[runs.n - 1] + (n - runs.first[runs.n - 1]) == base) {
+            // continues the previous run
+          } else if (runs.n < uint32_t(CodecBatch::kMaxRuns)) {
+            runs.first[runs.n] = uint32_t(n);
+            runs.slot[runs.n] = uint32_t(base);
+            ++runs.n;
+          } else {
+            fits = false;
+          }
+          for (uint64_t j = 0; j < cnt; ++j)
             ids[n++] = uint32_t(base + j);
         }
+    runs.first[runs.n] = uint32_t(n);
     const uint32_t* d_ids = nullptr;
+    const ChunkRuns* rp = nullptr;
     if (n != nchunks) {
-      CK(launch_stage_copy(d_chunk_ids[si], ids, n, se));
-      d_ids = d_chunk_ids[si];
+      if (fits) {
+        rp = &runs;
+      } else {
+        CK(launch_stage_copy(d_chunk_ids[si], ids, n, se));
+        d_ids = d_chunk_ids[si];
+      }
     }
     // the aggregation that read this compressed slot two batches ago must
     // be done before the encoders overwrite it
     CK(cudaStreamWaitEvent(se, ev_agg_done[si], 0));
     if (timed_begin(se, &metrics.compress, double(n * P.chunk_bytes), 0))
       return 1;
-    if (codec_compress(comp, n, d_ids, d_comp[si], d_sizes[si], codec_state[si], se))
+    if (codec_compress(comp, n, d_ids, rp, d_comp[si], d_sizes[si], codec_state[si], se))
       return 1;
     if (timed_end(se))
       return 1;

@@ -173,6 +173,7 @@ struct Stream
   int codec_compress(const uint8_t* pool,
                      uint64_t nchunks,
                      const uint32_t* d_ids,
+                     const ChunkRuns* runs,
                      uint8_t* out,
                      uint64_t* sizes,
                      void* scratch,
