@@ -513,6 +513,9 @@ void Stream::release()
       cudaFree(d_gather_tmp[si][l]);
       cudaFree(d_perm_tmp[si][l]);
       cudaFreeHost(h_lut_stage[si][l]);
+      d_gather_tmp[si][l] = d_perm_tmp[si][l] = nullptr;
+      h_lut_stage[si][l] = nullptr;
+      lut_eps[si][l].clear();
     }
   }
   if (s_copy)
@@ -731,12 +734,18 @@ int Stream::kick_batch(uint32_t n_epochs, const uint32_t* epoch_masks)
     const uint64_t n = uint64_t(na) * V.layout.chunks_per_epoch;
     if (!planned) {
       // staging of this delivery slot: its previous batch has been
-      // delivered, so its uploads are complete
-      uint32_t* hg = h_lut_stage[si][l];
-      uint32_t* hp = h_lut_stage[si][l] + n;
-      build_luts(l, na, eps, hg, hp);
-      CK(launch_stage_copy(d_gather_tmp[si][l], hg, n, su));
-      CK(launch_stage_copy(d_perm_tmp[si][l], hp, n, su));
+      // delivered, so its uploads are complete.  The tables depend only on
+      // the plan and the active epochs: the same pattern as this slot's
+      // last upload reuses them.
+      std::vector<uint32_t>& last = lut_eps[si][l];
+      if (last.size() != na || !std::equal(last.begin(), last.end(), eps)) {
+        uint32_t* hg = h_lut_stage[si][l];
+        uint32_t* hp = h_lut_stage[si][l] + n;
+        build_luts(l, na, eps, hg, hp);
+        CK(launch_stage_copy(d_gather_tmp[si][l], hg, n, su));
+        CK(launch_stage_copy(d_perm_tmp[si][l], hp, n, su));
+        last.assign(eps, eps + na);
+      }
       g = d_gather_tmp[si][l];
       pm = d_perm_tmp[si][l];
     }

@@ -109,6 +109,9 @@ struct Stream
   uint32_t* d_gather_tmp[2][LOD_MAX_LEVELS] = {};
   uint32_t* d_perm_tmp[2][LOD_MAX_LEVELS] = {};
   uint32_t* h_lut_stage[2][LOD_MAX_LEVELS] = {}; // per delivery slot
+  // active epochs of the tables last uploaded to d_gather_tmp/d_perm_tmp
+  // per slot and level (an unchanged pattern needs no new upload)
+  std::vector<uint32_t> lut_eps[2][LOD_MAX_LEVELS];
   uint32_t lut_cap[LOD_MAX_LEVELS] = {};
   uint32_t planned_count[LOD_MAX_LEVELS] = {};
   uint64_t* d_agg_scratch = nullptr;
