@@ -85,6 +85,27 @@ int main(int argc, char** argv)
     std::fprintf(stderr, "usage: codec_emu codec chunk_bytes n_chunks pattern seed\n");
     return 2;
   }
+  {
+    // slot runs of a partial batch (CodecBatch::id): entries 0-3 from slot
+    // 10, 4-5 from slot 40, 6-8 from slot 7; waves start at id_base
+    CodecBatch r{};
+    r.n_runs = 3;
+    const uint32_t first[4] = { 0, 4, 6, 9 }, slot[3] = { 10, 40, 7 };
+    for (int k = 0; k < 4; ++k)
+      r.run_first[k] = first[k];
+    for (int k = 0; k < 3; ++k)
+      r.run_slot[k] = slot[k];
+    const uint64_t want[9] = { 10, 11, 12, 13, 40, 41, 7, 8, 9 };
+    for (uint64_t base = 0; base < 9; ++base) {
+      r.id_base = base;
+      for (uint64_t i = 0; base + i < 9; ++i)
+        if (r.id(i) != want[base + i]) {
+          std::fprintf(stderr, "run mapping: entry %llu -> %llu\n",
+                       (unsigned long long)(base + i), (unsigned long long)r.id(i));
+          return 1;
+        }
+    }
+  }
   const std::string codec = argv[1];
   const uint32_t chunk = uint32_t(std::stoul(argv[2]));
   const uint64_t n = std::stoull(argv[3]);
