@@ -167,3 +167,36 @@ def make_config(dims, dtype="u16", codec="none", level=0, reduce="mean",
     cfg.shard_alignment = shard_alignment
     cfg.max_threads = max_threads
     return cfg
+
+
+# include/zarr_fs_sink.h (src/zarr_fs_sink.h:11-80)
+class ZarrConfig(C.Structure):
+    _fields_ = [("store_path", C.c_char_p), ("array_name", C.c_char_p),
+                ("data_type", C.c_int), ("fill_value", C.c_double),
+                ("rank", C.c_uint8), ("dimensions", C.POINTER(Dimension)),
+                ("unbuffered", C.c_int), ("codec", CodecConfig)]
+
+
+class ZarrMultiscaleConfig(C.Structure):
+    _fields_ = [("store_path", C.c_char_p), ("array_name", C.c_char_p),
+                ("data_type", C.c_int), ("fill_value", C.c_double),
+                ("rank", C.c_uint8), ("dimensions", C.POINTER(Dimension)),
+                ("nlod", C.c_int), ("unbuffered", C.c_int), ("codec", CodecConfig)]
+
+
+def bind_zarr_fs_sink(lib):
+    """Argument types of the fs-sink entry points of `lib` (this library, or
+    any other implementation of include/zarr_fs_sink.h)."""
+    P = C.c_void_p
+    lib.zarr_fs_sink_create.restype = P
+    lib.zarr_fs_sink_create.argtypes = [C.POINTER(ZarrConfig)]
+    lib.zarr_fs_multiscale_sink_create.restype = P
+    lib.zarr_fs_multiscale_sink_create.argtypes = [C.POINTER(ZarrMultiscaleConfig)]
+    for pre in ("zarr_fs_sink_", "zarr_fs_multiscale_sink_"):
+        getattr(lib, pre + "destroy").argtypes = [P]
+        getattr(lib, pre + "flush").argtypes = [P]
+        getattr(lib, pre + "pending_bytes").restype = C.c_size_t
+        getattr(lib, pre + "pending_bytes").argtypes = [P]
+        getattr(lib, pre + "as_shard_sink").restype = P
+        getattr(lib, pre + "as_shard_sink").argtypes = [P]
+    return lib

@@ -148,7 +148,8 @@ cudaError_t launch_stage_copy(uint32_t* dst, const uint32_t* src, uint64_t n,
   if (!n)
     return cudaSuccess;
   const uint64_t blocks = (n + 255) / 256;
-  stage_copy_k<<<int(blocks < 152 ? blocks : 152), 256, 0, st>>>(dst, src, n);
+  const uint64_t sms = uint64_t(device_sm_count());
+  stage_copy_k<<<int(blocks < sms ? blocks : sms), 256, 0, st>>>(dst, src, n);
   note_launches(1);
   return cudaGetLastError();
 }
@@ -169,7 +170,8 @@ cudaError_t launch_aggregate(const AggBatch& b,
   if (total) {
     const uint64_t ppc = (b.comp_stride + kPiece - 1) / kPiece;
     const uint64_t blocks = (total * ppc + 3) / 4;
-    const int grid = int(blocks < 152 * 64 ? blocks : 152 * 64);
+    const uint64_t cap = uint64_t(device_sm_count()) * 64;
+    const int grid = int(blocks < cap ? blocks : cap);
     agg_gather_k<<<grid, 128, 0, st>>>(b, total, ppc);
     note_launches(1);
   }

@@ -440,6 +440,27 @@ void note_launches(unsigned n)
 {
   g_launches += n;
 }
+
+// Streaming multiprocessors of the current device (cached per device; grid
+// caps are multiples of it).
+int device_sm_count()
+{
+  constexpr int kMaxDevices = 64;
+  static std::atomic<int> cache[kMaxDevices];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
+    return 1;
+  int n = cache[dev].load(std::memory_order_relaxed);
+  if (n > 0)
+    return n;
+  if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+      n <= 0) {
+    cudaGetLastError();
+    return 1;
+  }
+  cache[dev].store(n, std::memory_order_relaxed);
+  return n;
+}
 } // namespace chucky
 
 extern "C" uint64_t

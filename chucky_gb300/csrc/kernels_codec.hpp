@@ -10,6 +10,9 @@ namespace chucky {
 // Number of kernels this library has launched (process-wide).
 void note_launches(unsigned n);
 
+// Streaming multiprocessors of the current device.
+int device_sm_count();
+
 // Raw LZ4 blocks back to chunk bytes (a warp per block, bounds-checked):
 // block i is in_size[i] bytes at in + in_off[i] and decodes to chunk_bytes
 // bytes at out + i * out_stride; status[i] 0 when it did exactly that.

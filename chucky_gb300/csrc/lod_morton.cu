@@ -105,7 +105,7 @@ to_chunks_k(const T* __restrict__ values,
 inline int grid_for(uint64_t work)
 {
   const uint64_t blocks = (work + kThreads - 1) / kThreads;
-  const uint64_t cap = 152ull * 16;
+  const uint64_t cap = uint64_t(device_sm_count()) * 16;
   return int(blocks < cap ? (blocks ? blocks : 1) : cap);
 }
 

@@ -420,8 +420,8 @@ cudaError_t launch_drain_typed(const LodTileArgs& a, int l, uint32_t count,
 {
   const uint64_t n = a.lv[l].nelem * a.fixed_count;
   const uint64_t blocks = (n + 255) / 256;
-  const unsigned grid =
-    unsigned(blocks < 152 * 16 ? (blocks ? blocks : 1) : 152 * 16);
+  const uint64_t cap = uint64_t(device_sm_count()) * 16;
+  const unsigned grid = unsigned(blocks < cap ? (blocks ? blocks : 1) : cap);
   lod_drain_k<T, D><<<grid, 256, 0, st>>>(a, l, count);
   note_launches(1);
   return cudaGetLastError();

@@ -296,10 +296,15 @@ lz4_emit_k(CodecBatch b, const Seq* seqs, const SegMeta* meta)
 
 } // namespace
 
+// Saturates at SIZE_MAX when the product would overflow, so a caller that
+// compares the result with a fixed capacity rejects absurd chunk counts.
 size_t lz4_scratch_bytes(uint64_t n_chunks, uint32_t chunk_bytes)
 {
-  const uint64_t segs = n_chunks * ((chunk_bytes + kSegBytes - 1) / kSegBytes);
-  return segs * (kMaxSeqPerSeg * sizeof(Seq) + sizeof(SegMeta)) + 512;
+  const uint64_t per_chunk = ((uint64_t(chunk_bytes) + kSegBytes - 1) / kSegBytes) *
+                             (kMaxSeqPerSeg * sizeof(Seq) + sizeof(SegMeta));
+  if (per_chunk && n_chunks > (SIZE_MAX - 512) / per_chunk)
+    return SIZE_MAX;
+  return n_chunks * per_chunk + 512;
 }
 
 cudaError_t launch_lz4(CodecBatch b, void* scratch, cudaStream_t st)

@@ -5,10 +5,15 @@
 // The stream encodes chunks with launch_lz4 over scratch it allocates at
 // create (codec.cu); this entry point runs the same three kernels (find,
 // plan, emit) over caller-provided device input and output, with
-// `g_lz4_scratch` as scratch.  The array exists once per device (it is
-// allocated when the CUDA runtime loads this module into the device's
-// context); its address is looked up once per device, on the first call made
-// with that device current, and cached.
+// `g_lz4_scratch` as scratch.  The array exists once per CUDA context (it is
+// allocated when the CUDA runtime loads this module into the context, and
+// the primary context of each device is the usual one); its address is looked
+// up with cudaGetSymbolAddress on the first call made in a context and cached
+// together with that context's ID (cuCtxGetId: unique for the life of the
+// process, never reused).  A call made in another context -- another device,
+// a context a driver-API caller created and made current, or the new primary
+// context after cudaDeviceReset -- looks the address up again, so a stale
+// address from a destroyed context is never used.
 //
 // Every call rewrites all of the scratch it later reads (per-segment
 // sequences and metadata), so nothing in the array has to start at zero.
@@ -20,39 +25,102 @@
 
 #include <cuda_runtime.h>
 
-#include <atomic>
 #include <cstdio>
 #include <mutex>
 
 namespace {
 
 constexpr size_t kStaticScratchBytes = size_t(32) << 20;
-constexpr int kMaxDevices = 64;
+constexpr int kMaxCachedContexts = 64;
 
 __device__ __align__(256) unsigned char g_lz4_scratch[kStaticScratchBytes];
 
-std::mutex g_setup_mutex;
-std::atomic<void*> g_scratch_ptr[kMaxDevices];
+// cuCtxGetCurrent and cuCtxGetId, fetched through the runtime so that the
+// library does not link libcuda itself (CUresult is an int-sized enum,
+// CUcontext a pointer).
+using CtxGetCurrentFn = int (*)(void**);
+using CtxGetIdFn = int (*)(void*, unsigned long long*);
 
-void* scratch_for_current_device()
+struct CachedScratch
 {
-  int dev = -1;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
-    return nullptr;
-  void* p = g_scratch_ptr[dev].load(std::memory_order_acquire);
-  if (p)
-    return p;
-  std::lock_guard<std::mutex> lock(g_setup_mutex);
-  p = g_scratch_ptr[dev].load(std::memory_order_relaxed);
-  if (p)
-    return p;
-  if (cudaGetSymbolAddress(&p, g_lz4_scratch) != cudaSuccess || !p) {
-    std::fprintf(stderr,
-                 "chucky_gb300: static LZ4 scratch lookup failed on device %d: %s\n",
-                 dev, cudaGetErrorString(cudaGetLastError()));
+  unsigned long long ctx_id;
+  void* ptr;
+};
+
+std::mutex g_setup_mutex;
+CtxGetCurrentFn g_ctx_get_current = nullptr;
+CtxGetIdFn g_ctx_get_id = nullptr;
+bool g_driver_looked_up = false;
+CachedScratch g_cache[kMaxCachedContexts];
+int g_cache_used = 0;
+
+void* driver_entry(const char* name)
+{
+  void* fn = nullptr;
+  cudaDriverEntryPointQueryResult q{};
+  if (cudaGetDriverEntryPointByVersion(name, &fn, 12000, cudaEnableDefault, &q) !=
+        cudaSuccess ||
+      q != cudaDriverEntryPointSuccess) {
+    cudaGetLastError(); // clear a failed lookup
     return nullptr;
   }
-  g_scratch_ptr[dev].store(p, std::memory_order_release);
+  return fn;
+}
+
+// The ID of the calling thread's current context, or 0 when there is none
+// or the driver cannot tell (IDs start at 1).
+unsigned long long current_context_id()
+{
+  if (!g_driver_looked_up) {
+    g_driver_looked_up = true;
+    g_ctx_get_current = reinterpret_cast<CtxGetCurrentFn>(driver_entry("cuCtxGetCurrent"));
+    g_ctx_get_id = reinterpret_cast<CtxGetIdFn>(driver_entry("cuCtxGetId"));
+  }
+  void* ctx = nullptr;
+  unsigned long long id = 0;
+  if (!g_ctx_get_current || !g_ctx_get_id || g_ctx_get_current(&ctx) != 0 || !ctx ||
+      g_ctx_get_id(ctx, &id) != 0)
+    return 0;
+  return id;
+}
+
+void* scratch_for_current_context()
+{
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess)
+    return nullptr;
+  std::lock_guard<std::mutex> lock(g_setup_mutex);
+  unsigned long long id = current_context_id();
+  for (int i = 0; id && i < g_cache_used; ++i)
+    if (g_cache[i].ctx_id == id)
+      return g_cache[i].ptr;
+  // also makes the device's primary context current when the thread had no
+  // context yet
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_lz4_scratch);
+  if (e != cudaSuccess || !p) {
+    std::fprintf(stderr,
+                 "chucky_gb300: static LZ4 scratch lookup failed on device %d: %s\n",
+                 dev, cudaGetErrorString(e));
+    return nullptr;
+  }
+  if (!id)
+    id = current_context_id();
+  if (!id) {
+    std::fprintf(stderr,
+                 "chucky_gb300: static LZ4 scratch: the current CUDA context of "
+                 "device %d has no ID\n",
+                 dev);
+    return nullptr;
+  }
+  // the table keeps the most recent contexts (an evicted one that comes
+  // back is looked up again)
+  if (g_cache_used == kMaxCachedContexts) {
+    for (int i = 1; i < kMaxCachedContexts; ++i)
+      g_cache[i - 1] = g_cache[i];
+    --g_cache_used;
+  }
+  g_cache[g_cache_used++] = CachedScratch{ id, p };
   return p;
 }
 
@@ -100,7 +168,7 @@ chucky_lz4_encode_chunks_static(const void* d_chunks,
                  n_chunks, chunk_bytes, need, kStaticScratchBytes);
     return 2;
   }
-  void* scratch = scratch_for_current_device();
+  void* scratch = scratch_for_current_context();
   if (!scratch)
     return 3;
   chucky::CodecBatch b{};

@@ -52,7 +52,7 @@ int grid_for(uint64_t work)
 {
   // persistent-style grid: a multiple of the SM count, capped by the work
   const uint64_t blocks = (work + kThreads - 1) / kThreads;
-  const uint64_t cap = 152ull * 8;
+  const uint64_t cap = uint64_t(device_sm_count()) * 8;
   return int(blocks < cap ? (blocks ? blocks : 1) : cap);
 }
 

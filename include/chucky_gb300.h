@@ -50,10 +50,14 @@ extern "C"
    * cannot afford cudaFree's device-wide synchronisation or an
    * out-of-memory failure in the middle of a run.  The encoder's scratch is
    * a fixed array of chucky_lz4_static_scratch_bytes() (32 MiB) in device
-   * memory, set up once per device by the first call made with that device
-   * current (make that first call before anything that must not see setup
-   * work).  Requests needing more scratch than that -- about 10 MiB of
-   * input per call -- are rejected.
+   * memory, one per CUDA context (held until the context ends), set up by
+   * the first call made in that context (make that first call before any
+   * stream capture and before anything that must not see setup work).  The
+   * array's address is remembered per context ID, so calls after a
+   * cudaDeviceReset, on another device, or in a context a driver-API caller
+   * made current look it up again.  Requests needing more scratch than the
+   * array holds -- about 10 MiB of input per call -- are rejected, however
+   * large `n_chunks` is.
    *
    * Encodes `n_chunks` chunks of `chunk_bytes` each, chunk i at
    * d_chunks + i * in_stride (device memory, 4-byte aligned, `in_stride` a

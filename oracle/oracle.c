@@ -11,6 +11,7 @@
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+#include <time.h>
 
 #ifdef _OPENMP
 #include <omp.h>
@@ -1798,4 +1799,89 @@ uint64_t
 oracle_null_sink_bytes(const struct shard_sink* s)
 {
   return ((const struct o_null_sink*)s)->bytes;
+}
+
+/* ---- a stalling writer for writer_append_wait tests ---------------------- */
+
+struct oracle_stalling_writer
+{
+  struct writer base; /* first: the vtable callbacks recover the object */
+  int stalls, fail, calls;
+  size_t chunk;
+  double times[64];
+};
+
+static double
+stall_now(void)
+{
+  struct timespec ts;
+  clock_gettime(CLOCK_MONOTONIC, &ts);
+  return (double)ts.tv_sec + 1e-9 * (double)ts.tv_nsec;
+}
+
+static struct writer_result
+stalling_append(struct writer* self, struct slice data)
+{
+  struct oracle_stalling_writer* w = (struct oracle_stalling_writer*)self;
+  if (w->calls < 64)
+    w->times[w->calls] = stall_now();
+  w->calls++;
+  struct writer_result r = { 0, data };
+  if (w->calls <= w->stalls)
+    return r;
+  if (w->fail) {
+    r.error = writer_error_fail;
+    return r;
+  }
+  const size_t left = (size_t)((const char*)data.end - (const char*)data.beg);
+  const size_t take = (w->chunk && w->chunk < left) ? w->chunk : left;
+  r.rest.beg = (const char*)data.beg + take;
+  return r;
+}
+
+static struct writer_result
+stalling_flush(struct writer* self)
+{
+  (void)self;
+  struct writer_result r = { 0, { 0, 0 } };
+  return r;
+}
+
+struct oracle_stalling_writer*
+oracle_stalling_writer_create(int stalls, size_t chunk, int fail)
+{
+  struct oracle_stalling_writer* w =
+    (struct oracle_stalling_writer*)calloc(1, sizeof(*w));
+  if (!w)
+    return NULL;
+  w->base.append = stalling_append;
+  w->base.flush = stalling_flush;
+  w->stalls = stalls;
+  w->chunk = chunk;
+  w->fail = fail;
+  return w;
+}
+
+void
+oracle_stalling_writer_destroy(struct oracle_stalling_writer* w)
+{
+  free(w);
+}
+
+struct writer*
+oracle_stalling_writer_base(struct oracle_stalling_writer* w)
+{
+  return &w->base;
+}
+
+int
+oracle_stalling_writer_calls(const struct oracle_stalling_writer* w)
+{
+  return w->calls;
+}
+
+double
+oracle_stalling_writer_time(const struct oracle_stalling_writer* w, int call)
+{
+  return (call >= 0 && call < 64) ? w->times[call] : 0.0;
 }

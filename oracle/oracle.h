@@ -84,6 +84,20 @@ extern "C"
   void oracle_null_sink_destroy(struct shard_sink* s);
   uint64_t oracle_null_sink_bytes(const struct shard_sink* s);
 
+  /* A test writer for writer_append_wait: its append consumes nothing for
+   * the first `stalls` calls, then `chunk` bytes per call (everything when
+   * 0), or fails with writer_error_fail after the stalls when `fail`.  It
+   * records the monotonic time (seconds) of each of its first 64 calls. */
+  struct oracle_stalling_writer;
+  struct oracle_stalling_writer* oracle_stalling_writer_create(int stalls,
+                                                               size_t chunk,
+                                                               int fail);
+  void oracle_stalling_writer_destroy(struct oracle_stalling_writer* w);
+  struct writer* oracle_stalling_writer_base(struct oracle_stalling_writer* w);
+  int oracle_stalling_writer_calls(const struct oracle_stalling_writer* w);
+  double oracle_stalling_writer_time(const struct oracle_stalling_writer* w,
+                                     int call);
+
   /* crc32c (Castagnoli, reflected 0x82F63B78), as src/zarr/crc32c.c:5-28. */
   uint32_t oracle_crc32c(const void* data, size_t len);
 

@@ -300,3 +300,39 @@ def compare_decoded(cfg_codec, shards_codec, shards_raw, codec):
             comp_total += nc
             raw_total += nr
     return checked, comp_total, raw_total
+
+
+def run_into(impl, cfg, data, sink_base, pieces=None, quirks=True):
+    """Drive implementation `impl` ("oracle", "reference" or "gpu") into an
+    arbitrary shard_sink; returns the stream's final cursor."""
+    if impl == "oracle":
+        lib = oracle()
+        lib.oracle_set_reference_quirks(1 if quirks else 0)
+        try:
+            s = lib.oracle_stream_create(C.byref(cfg), sink_base)
+            if not s:
+                raise RuntimeError("oracle_stream_create failed")
+            try:
+                _drive(lib.oracle_stream_writer(s), data, pieces)
+                return lib.oracle_stream_cursor(s)
+            finally:
+                lib.oracle_stream_destroy(s)
+        finally:
+            lib.oracle_set_reference_quirks(1)
+    if impl == "reference":
+        lib = reference()
+        s = lib.tile_stream_cpu_create(C.byref(cfg), sink_base)
+        if not s:
+            raise RuntimeError("tile_stream_cpu_create failed")
+        try:
+            _drive(lib.tile_stream_cpu_writer(s), data, pieces)
+            return lib.tile_stream_cpu_cursor(s)
+        finally:
+            lib.tile_stream_cpu_destroy(s)
+    import chucky_gb300 as cg
+    s = cg.GpuStream(cfg, sink_base)
+    try:
+        _drive(s.writer, data, pieces)
+        return s.cursor()
+    finally:
+        s.close()

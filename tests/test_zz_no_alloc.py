@@ -65,13 +65,14 @@ def _stream_chunks(x, chunk_rows):
     return out
 
 
-def _static_chunks(lib, d_in, chunk_bytes, n_chunks, torch):
+def _static_chunks(lib, d_in, chunk_bytes, n_chunks, torch, offset=0, in_stride=None):
+    in_stride = in_stride or chunk_bytes
     out_stride = (_bound(chunk_bytes) + 255) // 256 * 256
     d_out = torch.empty(n_chunks * out_stride, dtype=torch.uint8, device="cuda")
     d_sizes = torch.zeros(n_chunks, dtype=torch.int64, device="cuda")
     st = torch.cuda.current_stream()
     rc = lib.chucky_lz4_encode_chunks_static(
-        d_in.data_ptr(), chunk_bytes, chunk_bytes, n_chunks,
+        d_in.data_ptr() + offset, chunk_bytes, in_stride, n_chunks,
         d_out.data_ptr(), out_stride, d_sizes.data_ptr(), st.cuda_stream)
     assert rc == 0
     st.synchronize()
@@ -112,6 +113,32 @@ def test_static_lz4_matches_stream_back_to_back():
             raw[(n_chunks - 1) * chunk_bytes: n_chunks * chunk_bytes].tobytes()
 
 
+@pytest.mark.gpu
+def test_static_lz4_gapped_input_at_a_4_byte_offset():
+    """Chunks 4 bytes past a 16-byte boundary with 12 bytes of other data
+    between them (in_stride = chunk_bytes + 12): the encoder's 4-byte input
+    path, checked against the stream's output for the same chunk bytes."""
+    torch = pytest.importorskip("torch")
+    lib = _lib()
+    x = _data(12, 40, 24578)  # 49156-byte chunks, one row each
+    expect = _stream_chunks(x, 1)
+    chunk_bytes = x.shape[1] * 2
+    n_chunks = x.shape[0]
+    stride = chunk_bytes + 12
+    rng = np.random.default_rng(3)
+    raw = rng.integers(0, 256, size=4 + n_chunks * stride + PAD, dtype=np.uint8)
+    rows = x.view(np.uint8).reshape(n_chunks, chunk_bytes)
+    for i in range(n_chunks):
+        raw[4 + i * stride: 4 + i * stride + chunk_bytes] = rows[i]
+    d_in = torch.from_numpy(raw).cuda()
+    for _ in range(2):
+        got = _static_chunks(lib, d_in, chunk_bytes, n_chunks, torch, offset=4,
+                             in_stride=stride)
+        assert len(got) == len(expect)
+        for i, (g, e) in enumerate(zip(got, expect)):
+            assert g == e, f"chunk {i}: {len(g)} vs {len(e)} bytes"
+
+
 def test_static_lz4_rejects_requests_beyond_the_fixed_scratch():
     lib = _lib()
     cap = lib.chucky_lz4_static_scratch_bytes()
@@ -127,3 +154,7 @@ def test_static_lz4_rejects_requests_beyond_the_fixed_scratch():
         fake + 1, chunk, chunk, 1, fake, _bound(chunk), fake, None) == 1  # misaligned
     assert lib.chucky_lz4_encode_chunks_static(
         fake, chunk, chunk, 0, fake, _bound(chunk), fake, None) == 0  # nothing to do
+    # chunk counts whose scratch size overflows 64 bits are rejected too
+    for n in (1 << 44, 1 << 50, (1 << 64) - 1):
+        assert lib.chucky_lz4_encode_chunks_static(
+            fake, chunk, chunk, n, fake, _bound(chunk), fake, None) == 2
