@@ -1,23 +1,36 @@
 """Pipeline ingest benchmark (one JSON line on stdout).
 
-Workload (the plain multiscale configuration): two 256^3 arrays streamed
-through the GPU writer back to back --
-  * u16, v = ((x ^ y ^ z) * 257 + U{0..15}) mod 65536, LOD mean;
-  * f32, v = sin(0.05 x) cos(0.07 y) z / 256 + N(0, 0.01), LOD median;
-z, y, x = 256, chunk 64^3, shard 4x4x4 chunks, 2x2x2 pyramid (z folded across
-epochs, dim-0 method mean; the level rule gives 3 levels), zstd level 3,
-discard sink.  Inputs are seeded synthetic data.
+Default workload (the served form against the plain one): 16 requests
+drawn (seeded) from four shapes -- the 256^3 u16 cube appended frame by
+frame, 2304 x 4096 u16 sensor frames (x32), 512^2 x 64 f32 stacks (x4),
+1024^2 u8 frames (x256) -- LZ4 / zstd-1 alternating, every other request
+with a 4-level mean pyramid, seeded synthetic data (4.8 GB per pass).
+  * served: a chucky_server (include/chucky_serve.h) with a 48 GB HBM
+    admission budget, up to 16 requests open at once, encoders batched
+    across streams; all 16 requests queued at once;
+  * plain: the same requests one at a time (max_streams 1, each stream
+    encoding on its own), appended as fast as possible.
+One step = one pass over the 16 requests (the request loop runs in C, one
+host thread per admitted request).  `value` / `e2e`: served GB/s of input
+with the inputs resident in HBM (stream-ordered device appends) / in pinned
+host memory (host-to-device copies inside the timed region); the plain form
+and the ratio beside them; p50 / p99 append-to-delivered latency per epoch
+from a pass with Poisson arrivals (mean gap 20 ms) and Poisson appends
+(mean gap 0.5 ms).
+  orca_e2e: one Orca-shaped stream -- 2304 x 4096 u16 frames, chunk
+    32 x 256 x 256, 5-level (t, y, x) max pyramid with dim-0 downsampling,
+    zstd-1 -- appended frame by frame from pinned host memory, as a
+    fraction of the pinned host-to-device link measured in the same run.
+  roofline: the dominant kernel set (the LZ4 encoder on sensor chunks)
+    timed alone with CUDA events (chucky_encode_chunks).
 
-One step = restart both streams (device buffers are kept), then one host
-thread per array appends the whole cube and flushes (every shard delivered
-to the sink); the two streams' GPU work overlaps.
-  value : inputs already resident in HBM (device pointers to append)
-  e2e   : the same from pinned host buffers (H2D inside the timed region)
-Both are GB/s of input bytes.  L2 is flushed (a 256 MiB write) between steps.
+Other workloads (`--workload`): multiscale (the 256^3 u16 + f32 pair,
+zstd-3), cube-lz4, sensor-zstd / sensor-lz4, batched (five rank-5 arrays).
 
 --impl reference times the CPU oracle of the same path (the reference's CPU
-algorithm restated in oracle/, zstd from the system libzstd) on all host
-cores, on a bounded sample of the workload (the u16 cube).
+algorithm restated in oracle/, LZ4-HC / zstd from the system libraries) on
+all host cores, on a bounded sample of the same workload (one request of
+each shape per step).
 
 Under torchrun (N > 1) every rank runs an independent replica ("replicas
 only": the path has no exchange step); value = all ranks' bytes / max time.
@@ -40,7 +53,8 @@ from chucky_gb300 import capi
 
 SIDE = 256
 CHUNK = 64
-METRIC = "pipeline ingest GB/s"
+METRIC = ("pipeline ingest GB/s (batched vs plain, 1 GB300, bit-exact round-trip); "
+          "p99 latency")
 
 
 def make_cubes(seed=7):
@@ -78,8 +92,7 @@ WORKLOAD = ("256^3 u16 (mean LOD) + 256^3 f32 (median LOD), chunk 64^3, shard "
             "(%d batches per array), discard sink"
             % (CUBE_EPOCHS_PER_BATCH, 4 // CUBE_EPOCHS_PER_BATCH))
 
-# Further workloads (`--workload`), each printing its own line; the default
-# line is the plain multiscale one above.
+# Further workloads (`--workload`), each printing its own line.
 SENSOR_H, SENSOR_W = 2304, 4096
 
 
@@ -497,6 +510,367 @@ def run_ours(args, rank, world):
     return line
 
 
+# ---------------------------------------------------------------------------
+# The served form against the plain one (the default line)
+# ---------------------------------------------------------------------------
+
+ORCA_FRAMES = 512
+SERVED_LINK_NOTE = ("pinned host->device copies of the same input buffers, measured "
+                    "right after the timed region")
+
+
+def _server_pass(srv, reqs, sink, paced=False):
+    import torch
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record()
+    srv.replay(reqs, sink, paced=paced)
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1)
+
+
+def served_form(reqs, lib, sink, max_streams, batch_encoders, steps, warmup,
+                budget=48 << 30):
+    """(ms per pass of the timed passes, discarded-sink bytes per pass,
+    launches, stats) of one form of the request loop."""
+    from chucky_gb300 import serve
+    with serve.Server(budget, max_streams, batch_encoders) as srv:
+        srv.prewarm(reqs, sink, per_request=max_streams > 1)
+        for _ in range(warmup):
+            srv.replay(reqs, sink, paced=False)
+        srv.reset_stats()
+        b0 = lib.chucky_discard_sink_bytes(sink)
+        l0 = lib.chucky_launch_count()
+        ms = [_server_pass(srv, reqs, sink) for _ in range(steps)]
+        launches = lib.chucky_launch_count() - l0
+        out_bytes = (lib.chucky_discard_sink_bytes(sink) - b0) / steps
+        st = srv.stats()
+    return ms, out_bytes, launches, st
+
+
+def served_latency(reqs, sink):
+    """One pass with Poisson arrivals and appends: latency and GB/s."""
+    from chucky_gb300 import serve
+    with serve.Server(48 << 30, 16, True) as srv:
+        srv.prewarm(reqs, sink, per_request=True)
+        srv.replay(reqs, sink, paced=False)
+        srv.reset_stats()
+        ms = _server_pass(srv, reqs, sink, paced=True)
+        st = srv.stats()
+    return ms, st
+
+
+def orca_e2e(lib, dev, steps):
+    """The Orca-shaped sensor stream (zstd-1, 5-level dim-0 max pyramid),
+    512 frames appended frame by frame from pinned host memory."""
+    import torch
+    import chucky_gb300 as cg
+    frames = sensor_frames(ORCA_FRAMES, dev)
+    dbuf = frames.reshape(-1).view(torch.uint8)
+    host = torch.empty(dbuf.numel(), dtype=torch.uint8, pin_memory=True)
+    host.copy_(dbuf)
+    sink = lib.chucky_discard_sink_create()
+    s = cg.GpuStream(sensor_config("zstd", "max"), sink)
+    frame = SENSOR_H * SENSOR_W * 2
+
+    def one():
+        if lib.tile_stream_gpu_restart(s.h, None) != 0:
+            raise RuntimeError("restart failed")
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        base = host.data_ptr()
+        for a in range(0, host.numel(), frame):
+            if s.append(base + a, frame).error:
+                raise RuntimeError("append failed")
+        if s.flush().error:
+            raise RuntimeError("flush failed")
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1)
+
+    for _ in range(2):
+        one()
+    ms = [one() for _ in range(steps)]
+    link = h2d_probe([host], [dbuf], dev)
+    s.close()
+    lib.chucky_discard_sink_destroy(sink)
+    gbs = host.numel() * len(ms) / (sum(ms) * 1e-3) / 1e9
+    out = {"workload": "%d u16 frames 2304x4096 (seeded Poisson(100) + 64 Gaussian blobs), "
+                       "chunk 32x256x256, shard 32x2048x2048, 5-level (t,y,x) max pyramid "
+                       "with dim-0 downsampling, zstd-1, K=%d, appended frame by frame from "
+                       "pinned host memory" % (ORCA_FRAMES, EPOCHS_PER_BATCH),
+           "value": round(gbs, 3), "unit": "GB/s", "steps": len(ms),
+           "ms_per_step": round(float(np.mean(ms)), 3),
+           "h2d_link_gbs": round(link, 2), "link_note": SERVED_LINK_NOTE,
+           "frac_of_h2d_link": round(gbs / link, 4) if link else None}
+    del frames, dbuf, host
+    torch.cuda.empty_cache()
+    return out
+
+
+def encoder_roofline(lib, dev, codec="lz4", reps=5):
+    """The encoder launch set alone on one 256 MiB batch of sensor chunks
+    (64 chunks of 32 x 256 x 256 u16), CUDA events on its stream: bytes
+    read + written per launch set and the chunk-input rate."""
+    import torch
+    f = lib.chucky_encode_chunks
+    f.restype = C.c_int
+    f.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_size_t, C.c_size_t, C.c_size_t,
+                  C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p]
+    lib.chucky_encode_bound.restype = C.c_size_t
+    lib.chucky_encode_bound.argtypes = [C.c_int, C.c_size_t]
+    lib.chucky_encode_scratch_bytes.restype = C.c_size_t
+    lib.chucky_encode_scratch_bytes.argtypes = [C.c_int, C.c_size_t, C.c_size_t]
+    cid = capi.CODEC[codec]
+    frames = sensor_frames(64, dev)  # 64 frames: 2 epochs of 9 x 16 chunk tiles
+    # chunk tiles 32 x 256 x 256 of the first 64 frames, as the stream lays them out
+    t = frames.reshape(2, 32, 9, 256, 16, 256).permute(0, 2, 4, 1, 3, 5).contiguous()
+    chunk_bytes = 32 * 256 * 256 * 2
+    n = 64
+    chunks = t.reshape(-1).view(torch.uint8)[: n * chunk_bytes]
+    pad = torch.zeros(n * chunk_bytes + 256, dtype=torch.uint8, device=dev)
+    pad[: n * chunk_bytes].copy_(chunks)
+    bound = lib.chucky_encode_bound(cid, chunk_bytes)
+    out_stride = (bound + 15) // 16 * 16
+    out = torch.empty(n * out_stride, dtype=torch.uint8, device=dev)
+    sizes = torch.zeros(n, dtype=torch.int64, device=dev)
+    sb = lib.chucky_encode_scratch_bytes(cid, chunk_bytes, n)
+    scratch = torch.empty(sb, dtype=torch.uint8, device=dev)
+    st = torch.cuda.Stream(device=dev)
+    level = 1
+    times = []
+    for r in range(reps + 2):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(st)
+        rc = f(cid, level, pad.data_ptr(), chunk_bytes, chunk_bytes, n, out.data_ptr(),
+               out_stride, sizes.data_ptr(), scratch.data_ptr(), sb, st.cuda_stream)
+        e1.record(st)
+        st.synchronize()
+        if rc:
+            raise RuntimeError("chucky_encode_chunks failed")
+        if r >= 2:
+            times.append(e0.elapsed_time(e1))
+    comp = int(sizes.sum().item())
+    ms = float(np.mean(times))
+    del frames, t, chunks, pad, out, scratch
+    torch.cuda.empty_cache()
+    return {"input_bytes": n * chunk_bytes, "output_bytes": comp, "ms": ms,
+            "input_gbs": n * chunk_bytes / (ms * 1e-3) / 1e9,
+            "achieved_gbs": (n * chunk_bytes + comp) / (ms * 1e-3) / 1e9}
+
+
+# DRAM bytes (read + written) per byte of chunk input of the LZ4 launch set
+# on sensor chunks, from the ncu capture summarised in
+# profiles/lz4_encoder_sensor_chunks.md (scaled to the launch's input)
+LZ4_SENSOR_TRAFFIC_PER_INPUT_BYTE = None
+
+
+def run_served_bench(args, rank, world):
+    import torch
+    import chucky_gb300 as cg
+    from chucky_gb300 import build as cgbuild, serve
+    cgbuild.build()
+    lib = serve._lib()
+    lib.tile_stream_gpu_restart.argtypes = [C.c_void_p, C.c_void_p]
+    lib.chucky_launch_count.restype = C.c_uint64
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    torch.cuda.set_device(dev)
+    sink = lib.chucky_discard_sink_create()
+    import dataclasses
+    host_reqs = serve.c5_requests()                   # pinned host inputs
+    on_dev = {}
+    for r in host_reqs:                               # HBM-resident copies
+        if id(r.data) not in on_dev:
+            on_dev[id(r.data)] = r.data.to(dev)
+    dev_reqs = [dataclasses.replace(r, data=on_dev[id(r.data)], _cfg=None)
+                for r in host_reqs]
+    nbytes = sum(r.buffer()[1] for r in host_reqs)
+
+    clocks = Clocks()
+    if rank == 0:
+        clocks.start()
+    ms_dev, out_b, launches, st_dev = served_form(dev_reqs, lib, sink, 16, True,
+                                                   args.steps, args.warmup)
+    ms_host, out_h, _, st_host = served_form(host_reqs, lib, sink, 16, True,
+                                             args.steps, max(1, args.warmup // 2))
+    clk = clocks.stop() if rank == 0 else None
+    pms_dev, _, _, _ = served_form(dev_reqs, lib, sink, 1, False, args.steps, args.warmup)
+    pms_host, _, _, _ = served_form(host_reqs, lib, sink, 1, False, args.steps,
+                                    max(1, args.warmup // 2))
+    lat_ms, lat = served_latency(host_reqs, sink)
+    link = h2d_probe([r.data for r in host_reqs[:4]], [r.data for r in dev_reqs[:4]], dev)
+    lib.chucky_discard_sink_destroy(sink)
+    del dev_reqs
+    torch.cuda.empty_cache()
+    orca = orca_e2e(lib, dev, max(3, args.steps // 2))
+    enc = encoder_roofline(lib, dev, "lz4")
+    enc_z = encoder_roofline(lib, dev, "zstd")
+
+    totals = max_over_ranks([float(np.sum(ms_dev)), float(np.sum(ms_host)),
+                             float(np.sum(pms_dev)), float(np.sum(pms_host))], world, dev)
+    value, e2e, pvalue, pe2e = (whole_job_gbs(nbytes, args.steps, world, t) for t in totals)
+    if rank != 0:
+        return None
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    peak, peak_src = 6800.0, "fallback"
+    if os.path.exists(peaks_path):
+        peak = float(json.load(open(peaks_path))["hbm_gbs"])
+        peak_src = "measured"
+    traffic = (round(LZ4_SENSOR_TRAFFIC_PER_INPUT_BYTE * enc["input_bytes"])
+               if LZ4_SENSOR_TRAFFIC_PER_INPUT_BYTE else None)
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": "GB/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(totals[0] / args.steps, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u8+u16+f32",
+        "data": "synthetic (seeded: Poisson(100) u16 frames, N(0,1) f32 stacks, "
+                "uniform u8 frames)",
+        "config": {"workload": "served form: " + serve.C5_WORKLOAD,
+                   "input_bytes_per_step": nbytes,
+                   "l2": "inputs larger than L2 (4.8 GB per step)",
+                   "parallelism": f"replicas x{world}",
+                   "served": "chucky_server, 48 GB budget, up to 16 requests open, "
+                             "encoders batched across streams, all requests queued",
+                   "plain": "the same requests one at a time, each stream encoding on "
+                            "its own"},
+        "e2e": {"value": round(e2e, 3), "unit": "GB/s",
+                "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": int(out_h),
+                "ms_per_step": round(totals[1] / args.steps, 3),
+                "h2d_link_gbs": round(link, 2), "frac_of_h2d_link": round(e2e / link, 4)},
+        "plain": {"value": round(pvalue, 3), "e2e": round(pe2e, 3), "unit": "GB/s"},
+        "served_over_plain": {"value": round(value / pvalue, 3),
+                              "e2e": round(e2e / pe2e, 3)},
+        "latency": {"p50_ms": round(lat["p50_ms"], 3), "p99_ms": round(lat["p99_ms"], 3),
+                    "max_ms": round(lat["max_ms"], 3), "epochs": lat["epochs"],
+                    "gbs": round(lat["input_bytes"] / (lat_ms * 1e-3) / 1e9, 3),
+                    "arrivals": "Poisson, mean gap 20 ms; appends Poisson, mean gap "
+                                "0.5 ms; pinned host inputs",
+                    "definition": "append of an epoch's last byte to the end of the "
+                                  "sink writes of its batch"},
+        "served_stats": {k: st_dev[k] for k in (
+            "peak_open", "peak_resident_bytes", "streams_created", "streams_reused",
+            "engine_rounds", "engine_jobs", "engine_launch_sets",
+            "engine_max_jobs_per_round")},
+        "compression_ratio": round(nbytes / max(1.0, out_b), 4),
+        "orca_e2e": orca,
+        "roofline": {"kernel": "lz4 encoder launch set (find+plan+emit) on 64 sensor "
+                               "chunks of 32x256x256 u16, timed alone",
+                     "bound": "hbm", "limiter": "compute (match finding and sequence "
+                                                "emission; not bandwidth)",
+                     "achieved": round(enc["achieved_gbs"], 2), "peak": peak,
+                     "unit": "GB/s", "frac": round(enc["achieved_gbs"] / peak, 4),
+                     "peak_source": peak_src, "traffic": traffic,
+                     "traffic_note": ("ncu DRAM bytes of the same launch set, per launch"
+                                      if traffic else "not captured"),
+                     "input_gbs": round(enc["input_gbs"], 2),
+                     "ms_per_launch_set": round(enc["ms"], 4)},
+        "roofline_zstd": {"kernel": "zstd encoder launch set (find+table+block+frame), "
+                                    "same chunks, timed alone",
+                          "achieved": round(enc_z["achieved_gbs"], 2),
+                          "frac": round(enc_z["achieved_gbs"] / peak, 4),
+                          "input_gbs": round(enc_z["input_gbs"], 2),
+                          "ms_per_launch_set": round(enc_z["ms"], 4)},
+        "gpu_launches": int(launches),
+        "clocks": clk,
+    }
+    if args.cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline_served(args)
+    return line
+
+
+def cpu_request_step(req, threads):
+    """One request through the oracle (the whole array in one append)."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import harness as H
+    lib = H.oracle()
+    sink = lib.oracle_null_sink_create()
+    cfg = req.config()
+    cfg.max_threads = threads
+    s = lib.oracle_stream_create(C.byref(cfg), sink)
+    if not s:
+        raise RuntimeError("oracle stream create failed")
+    data = req.data.numpy() if hasattr(req.data, "numpy") else req.data
+    buf = np.ascontiguousarray(data).view(np.uint8).reshape(-1)
+    t0 = time.perf_counter()
+    wp = lib.oracle_stream_writer(s)
+    r = wp.contents.append(wp, capi.Slice(buf.ctypes.data, buf.ctypes.data + buf.size))
+    if r.error or wp.contents.flush(wp).error:
+        raise RuntimeError("oracle stream failed")
+    dt = time.perf_counter() - t0
+    lib.oracle_stream_destroy(s)
+    lib.oracle_null_sink_destroy(sink)
+    return dt, buf.size
+
+
+def served_sample():
+    """One request of each of the four shapes (as drawn for the workload)."""
+    from chucky_gb300 import serve
+    reqs = serve.c5_requests(pinned=False)
+    out, seen = [], set()
+    for r in reqs:
+        kind = r.name.split(":")[1]
+        if kind not in seen:
+            seen.add(kind)
+            out.append(r)
+    return out
+
+
+def cpu_baseline_served(args):
+    threads = os.cpu_count() or 1
+    sample = served_sample()
+    tot_t, tot_b, passes = 0.0, 0, 0
+    while passes < 5 and (passes < 1 or tot_t < 10.0):
+        for r in sample:
+            dt, nb = cpu_request_step(r, threads)
+            tot_t += dt
+            tot_b += nb
+        passes += 1
+    return {"value": round(tot_b / tot_t / 1e9, 4), "unit": "GB/s", "cores": threads,
+            "kind": "port",
+            "sample": f"{passes} pass(es) over one request of each of the four shapes "
+                      f"({', '.join(r.name for r in sample)}; {tot_b / passes / 1e9:.2f} GB "
+                      f"per pass, {tot_t:.1f} s) through the oracle/ restatement of the "
+                      "reference CPU backend (LZ4-HC / zstd from the system libraries)"}
+
+
+def run_reference_served(args, rank, world):
+    if rank != 0:
+        return None
+    threads = os.cpu_count() or 1
+    sample = served_sample()
+    for _ in range(args.warmup):
+        cpu_request_step(sample[-1], threads)
+    tot_t, tot_b = 0.0, 0
+    for _ in range(args.steps):
+        for r in sample:
+            dt, nb = cpu_request_step(r, threads)
+            tot_t += dt
+            tot_b += nb
+    v = tot_b / tot_t / 1e9
+    from chucky_gb300 import serve
+    desc = ("served form: " + serve.C5_WORKLOAD)
+    return {"impl": "reference", "metric": METRIC, "value": round(v, 4), "unit": "GB/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(tot_t / args.steps * 1e3, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "u8+u16+f32", "data": "synthetic",
+            "config": {"workload": desc, "same_config": True,
+                       "sample": "each step: one request of each of the four shapes "
+                                 "(bounded CPU sample of the same workload)"},
+            "cpu_baseline": {"value": round(v, 4), "unit": "GB/s", "cores": threads,
+                             "kind": "port",
+                             "sample": "one request per shape per step through the "
+                                       "oracle/ restatement of the reference CPU backend"},
+            "e2e": {"value": round(v, 4), "unit": "GB/s",
+                    "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
 def cpu_oracle_step(cube, cfg, threads):
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     import harness as H
@@ -610,10 +984,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
-    ap.add_argument("--workload", default="multiscale",
-                    choices=["multiscale", "cube-lz4", "sensor-zstd", "sensor-lz4",
-                             "batched"],
-                    help="multiscale: the plain multiscale line (default); cube-lz4: "
+    ap.add_argument("--workload", default="served",
+                    choices=["served", "multiscale", "cube-lz4", "sensor-zstd",
+                             "sensor-lz4", "batched"],
+                    help="served: the served form against the plain one (default); "
+                         "multiscale: the 256^3 u16 + f32 pair; cube-lz4: "
                          "the 256^3 u16 cube with LZ4 and no LOD; sensor-*: 2304x4096 "
                          "u16 frames with a 5-level dim-0 pyramid; batched: five rank-5 "
                          "arrays of different dtypes with uneven chunk classes")
@@ -634,7 +1009,10 @@ def main():
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
         dist.init_process_group("nccl")
     if args.impl == "reference":
-        line = run_reference(args, rank, world)
+        line = (run_reference_served(args, rank, world) if args.workload == "served"
+                else run_reference(args, rank, world))
+    elif args.workload == "served":
+        line = run_served_bench(args, rank, world)
     else:
         line = run_ours(args, rank, world)
     if world > 1:

@@ -200,3 +200,48 @@ def bind_zarr_fs_sink(lib):
         getattr(lib, pre + "as_shard_sink").restype = P
         getattr(lib, pre + "as_shard_sink").argtypes = [P]
     return lib
+
+
+# include/chucky_serve.h (served form; no reference counterpart)
+class ServerConfig(C.Structure):
+    _fields_ = [("hbm_budget_bytes", C.c_size_t), ("max_streams", C.c_int),
+                ("batch_encoders", C.c_int), ("encoder_wave_bytes", C.c_size_t)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("requests", C.c_uint64), ("input_bytes", C.c_uint64),
+                ("epochs", C.c_uint64), ("p50_ms", C.c_double), ("p99_ms", C.c_double),
+                ("max_ms", C.c_double), ("streams_created", C.c_uint64),
+                ("streams_reused", C.c_uint64), ("streams_evicted", C.c_uint64),
+                ("peak_resident_bytes", C.c_uint64), ("peak_open", C.c_uint64),
+                ("engine_rounds", C.c_uint64), ("engine_jobs", C.c_uint64),
+                ("engine_launch_sets", C.c_uint64),
+                ("engine_max_jobs_per_round", C.c_uint64)]
+
+
+class ReplayRequest(C.Structure):
+    _fields_ = [("config", C.POINTER(StreamConfiguration)), ("sink", C.c_void_p),
+                ("data", C.c_void_p), ("bytes", C.c_size_t), ("append_bytes", C.c_size_t),
+                ("arrival_s", C.c_double), ("mean_gap_s", C.c_double),
+                ("seed", C.c_uint64)]
+
+
+def bind_server(lib):
+    """Argument types of the served-form entry points."""
+    P = C.c_void_p
+    lib.chucky_server_create.restype = P
+    lib.chucky_server_create.argtypes = [C.POINTER(ServerConfig)]
+    lib.chucky_server_destroy.argtypes = [P]
+    lib.chucky_server_open.restype = P
+    lib.chucky_server_open.argtypes = [P, C.POINTER(StreamConfiguration), P, C.c_int]
+    lib.chucky_request_writer.restype = C.POINTER(Writer)
+    lib.chucky_request_writer.argtypes = [P]
+    lib.chucky_request_close.argtypes = [P]
+    lib.chucky_server_get_stats.argtypes = [P, C.POINTER(ServerStats)]
+    lib.chucky_server_reset_stats.argtypes = [P]
+    lib.chucky_server_replay.argtypes = [P, C.POINTER(ReplayRequest), C.c_size_t,
+                                         C.POINTER(C.c_double)]
+    lib.chucky_server_prewarm.restype = C.c_size_t
+    lib.chucky_server_prewarm.argtypes = [P, C.POINTER(C.POINTER(StreamConfiguration)),
+                                          C.c_size_t, P]
+    return lib

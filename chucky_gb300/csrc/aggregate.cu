@@ -6,7 +6,8 @@
 //      covering positions are 0;
 //   2. the pre-padding sizes are kept for the shard index;
 //   3. the last chunk of each shard group (n_active * cps_inner positions)
-//      absorbs the padding that rounds the group to the shard alignment;
+//      absorbs the padding that rounds the group to the shard alignment,
+//      which is written as zeros;
 //   4. exclusive scan -> byte offsets (offsets[positions] = total);
 //   5. every chunk's bytes are copied to out + offsets[perm[i]].
 // Steps 1-4 run in one CTA per level (a few thousand positions); step 5
@@ -91,6 +92,18 @@ agg_layout_k(AggBatch b, uint64_t* scratch, uint64_t scratch_stride)
   }
   if (threadIdx.x == 0)
     L.offsets[L.positions] = carry;
+  // the padding that rounds each shard group up to the alignment is written
+  // as zeros (no stale buffer bytes reach the shard files)
+  if (b.alignment > 0 && L.group > 0) {
+    __syncthreads();
+    for (uint64_t g = 0; g < L.positions / L.group; ++g) {
+      const uint64_t last = g * L.group + L.group - 1;
+      const uint64_t beg = L.offsets[last] + L.real_sizes[last];
+      const uint64_t end = L.offsets[last + 1];
+      for (uint64_t q = beg + threadIdx.x; q < end; q += blockDim.x)
+        L.out[q] = 0;
+    }
+  }
 }
 
 // One warp per 16 KiB piece of one chunk: (chunk, piece) pairs are spread
@@ -131,6 +144,24 @@ __global__ void fill_u64_k(uint64_t* p, uint64_t v, uint64_t n)
   for (uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; i < n;
        i += uint64_t(gridDim.x) * blockDim.x)
     p[i] = v;
+}
+
+// Bytes [start, *total) of each level's device copy to its host slot (the
+// part the copy engine's transfer of the expected size did not cover), a
+// 64 KiB piece per CTA and step; levels along grid y.
+constexpr uint64_t kTailPiece = 64 << 10;
+
+__global__ void __launch_bounds__(256) tail_copy_k(TailCopies t)
+{
+  const TailCopy& c = t.lv[blockIdx.y];
+  const uint64_t total = *c.total;
+  if (total <= c.start)
+    return;
+  for (uint64_t p = c.start + blockIdx.x * kTailPiece; p < total;
+       p += uint64_t(gridDim.x) * kTailPiece) {
+    const uint64_t n = total - p < kTailPiece ? total - p : kTailPiece;
+    copy_bytes(c.dst + p, c.src + p, n, threadIdx.x, blockDim.x);
+  }
 }
 
 __global__ void stage_copy_k(uint32_t* dst, const uint32_t* src, uint64_t n)
@@ -175,6 +206,18 @@ cudaError_t launch_aggregate(const AggBatch& b,
     agg_gather_k<<<grid, 128, 0, st>>>(b, total, ppc);
     note_launches(1);
   }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_tail_copy(const TailCopies& t, uint64_t max_bytes, cudaStream_t st)
+{
+  if (t.n <= 0 || !max_bytes)
+    return cudaSuccess;
+  const uint64_t pieces = (max_bytes + kTailPiece - 1) / kTailPiece;
+  const uint64_t cap = uint64_t(device_sm_count()) * 2;
+  const dim3 grid(unsigned(pieces < cap ? pieces : cap), unsigned(t.n));
+  tail_copy_k<<<grid, 256, 0, st>>>(t);
+  note_launches(1);
   return cudaGetLastError();
 }
 

@@ -343,9 +343,13 @@ chucky_crc32c(const void* data, size_t len)
 
 // ---- memory estimate / chunk advice (replace src/gpu/stream.init.c:321-488)
 
-extern "C" int
-tile_stream_gpu_memory_estimate(const tile_stream_configuration* config,
-                                tile_stream_memory_info* info)
+namespace chucky {
+
+// `shared_encoder`: the stream encodes through a server's engine and holds
+// no encoder scratch of its own.
+int estimate_stream(const tile_stream_configuration* config,
+                    tile_stream_memory_info* info,
+                    bool shared_encoder)
 {
   if (!info)
     return 1;
@@ -382,11 +386,16 @@ tile_stream_gpu_memory_estimate(const tile_stream_configuration* config,
     uint64_t values = 0;
     for (int l = 0; l < P.nlod; ++l)
       values += P.fixed_count * P.lv[l].lod_nelem;
-    info->lod_bytes = values * P.bpe * (P.append_downsample ? 2 : 1) +
-                      P.ends.size() * 8 + P.lv[0].lod_nelem * 4 +
+    // dim-0 accumulators (levels >= 1), per-slice offsets; the general path
+    // adds Morton-ordered level buffers, window ends and LUTs
+    const uint64_t above0 = values - P.fixed_count * P.lv[0].lod_nelem;
+    info->lod_bytes = (P.append_downsample ? above0 * P.bpe : 0) +
                       P.fixed_count * 8 * uint64_t(P.nlod + 1);
-    for (int l = 0; l < P.nlod; ++l)
-      info->lod_bytes += P.lv[l].lod_nelem * 4;
+    if (!chucky::lod_plan_is_tiled(P)) {
+      info->lod_bytes += values * P.bpe + P.n_ends * 8 + P.lv[0].lod_nelem * 4;
+      for (int l = 0; l < P.nlod; ++l)
+        info->lod_bytes += P.lv[l].lod_nelem * 4;
+    }
   }
   {
     // encoder scratch of one wave (256 MiB of input per encoder launch)
@@ -397,19 +406,30 @@ tile_stream_gpu_memory_estimate(const tile_stream_configuration* config,
       scratch = chucky::zstd_scratch_bytes(wave, uint32_t(P.chunk_bytes));
     else if (config->codec.id == CODEC_LZ4_NON_STANDARD)
       scratch = chucky::lz4_scratch_bytes(wave, uint32_t(P.chunk_bytes));
-    info->codec_bytes = 2 * nchunks * 8 + 2 * scratch; // one scratch per slot
+    info->codec_bytes =
+      2 * nchunks * 8 + (shared_encoder ? 0 : 2 * scratch); // one scratch per slot
   }
   info->shard_bytes = shard;
   info->device_bytes = info->staging_bytes + info->chunk_pool_bytes +
                        info->compressed_pool_bytes + info->aggregate_bytes +
                        info->lod_bytes + info->codec_bytes;
-  info->host_pinned_bytes = agg_host;
+  info->host_pinned_bytes =
+    agg_host + chucky::kStreamStageSlots * chucky::staging_slot_bytes(config->buffer_capacity_bytes);
   info->chunks_per_epoch = P.lv[0].layout.chunks_per_epoch;
   info->total_chunks = P.total_chunks;
   info->max_output_size = P.max_out;
   info->nlod = P.nlod;
   info->epochs_per_batch = P.K;
   return 0;
+}
+
+} // namespace chucky
+
+extern "C" int
+tile_stream_gpu_memory_estimate(const tile_stream_configuration* config,
+                                tile_stream_memory_info* info)
+{
+  return chucky::estimate_stream(config, info, false);
 }
 
 extern "C" int

@@ -31,6 +31,13 @@ int Stream::codec_init()
     if (cudaHostAlloc(&h_chunk_ids[i], n * 4, cudaHostAllocMapped) != cudaSuccess ||
         cudaMalloc(&d_chunk_ids[i], n * 4) != cudaSuccess)
       return 1;
+  if (engine) { // the engine owns the scratch
+    for (int i = 0; i < 2; ++i)
+      if (cudaEventCreateWithFlags(&ev_engine_done[i], cudaEventDisableTiming) !=
+          cudaSuccess)
+        return 1;
+    return 0;
+  }
   for (int i = 0; i < 2; ++i)
     if (cudaMalloc(&codec_state[i], bytes) != cudaSuccess)
       return 1;
@@ -93,6 +100,9 @@ void Stream::codec_release()
   for (int i = 0; i < 2; ++i) {
     cudaFree(codec_state[i]);
     codec_state[i] = nullptr;
+    if (ev_engine_done[i])
+      cudaEventDestroy(ev_engine_done[i]);
+    ev_engine_done[i] = nullptr;
   }
   for (int i = 0; i < 2; ++i) {
     cudaFreeHost(h_chunk_ids[i]);
@@ -103,3 +113,72 @@ void Stream::codec_release()
 }
 
 } // namespace chucky
+
+// ---- batched chunk encoding as a library call -------------------------------
+// (the batch-level counterpart of the reference's codec_compress,
+// src/gpu/compress.cu:284-369, which calls nvcomp)
+
+extern "C" size_t
+chucky_encode_bound(int codec_id, size_t chunk_bytes)
+{
+  if (codec_id != CODEC_LZ4_NON_STANDARD && codec_id != CODEC_ZSTD)
+    return 0;
+  return size_t(chucky::codec_bound(codec_id, chunk_bytes));
+}
+
+extern "C" size_t
+chucky_encode_scratch_bytes(int codec_id, size_t chunk_bytes, size_t n_chunks)
+{
+  if (!chunk_bytes || chunk_bytes >= (size_t(1) << 32))
+    return 0;
+  if (codec_id == CODEC_ZSTD)
+    return chucky::zstd_scratch_bytes(n_chunks, uint32_t(chunk_bytes));
+  if (codec_id == CODEC_LZ4_NON_STANDARD)
+    return chucky::lz4_scratch_bytes(n_chunks, uint32_t(chunk_bytes));
+  return 0;
+}
+
+extern "C" int
+chucky_encode_chunks(int codec_id,
+                     int level,
+                     const void* d_chunks,
+                     size_t chunk_bytes,
+                     size_t in_stride,
+                     size_t n_chunks,
+                     void* d_out,
+                     size_t out_stride,
+                     uint64_t* d_sizes,
+                     void* d_scratch,
+                     size_t scratch_bytes,
+                     void* cuda_stream)
+{
+  if (!n_chunks)
+    return 0;
+  if ((codec_id != CODEC_LZ4_NON_STANDARD && codec_id != CODEC_ZSTD) || !d_chunks ||
+      !d_out || !d_sizes || !d_scratch || !chunk_bytes ||
+      chunk_bytes >= (size_t(1) << 32) || in_stride < chunk_bytes ||
+      (reinterpret_cast<uintptr_t>(d_chunks) & 3) || (in_stride & 3) ||
+      out_stride < chucky::codec_bound(codec_id, chunk_bytes) ||
+      scratch_bytes < chucky_encode_scratch_bytes(codec_id, chunk_bytes, n_chunks)) {
+    std::fprintf(stderr, "chucky_gb300: chucky_encode_chunks: invalid arguments\n");
+    return 1;
+  }
+  chucky::CodecBatch b{};
+  b.in = static_cast<const uint8_t*>(d_chunks);
+  b.in_stride = in_stride;
+  b.chunk_bytes = uint32_t(chunk_bytes);
+  b.n_chunks = n_chunks;
+  b.out = static_cast<uint8_t*>(d_out);
+  b.out_stride = out_stride;
+  b.out_sizes = d_sizes;
+  b.level = level;
+  const cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);
+  const cudaError_t e = codec_id == CODEC_ZSTD ? chucky::launch_zstd(b, d_scratch, st)
+                                               : chucky::launch_lz4(b, d_scratch, st);
+  if (e != cudaSuccess) {
+    std::fprintf(stderr, "chucky_gb300: chucky_encode_chunks: %s\n",
+                 cudaGetErrorString(e));
+    return 3;
+  }
+  return 0;
+}

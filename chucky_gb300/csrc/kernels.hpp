@@ -136,6 +136,24 @@ cudaError_t launch_aggregate(const AggBatch& b,
                              uint64_t* scratch, // >= max positions
                              cudaStream_t st);
 
+// The rest of a batch's shard-ordered bytes after a copy-engine transfer of
+// the expected size: per level, bytes [start, *total) of `src` (device) to
+// `dst` (mapped host memory), where *total is the level's byte count the
+// aggregation wrote on the device.  `max_bytes` bounds total - start.
+struct TailCopy
+{
+  uint8_t* dst;
+  const uint8_t* src; // readable 20 bytes past *total
+  const uint64_t* total;
+  uint64_t start;
+};
+struct TailCopies
+{
+  int n;
+  TailCopy lv[32];
+};
+cudaError_t launch_tail_copy(const TailCopies& t, uint64_t max_bytes, cudaStream_t st);
+
 cudaError_t launch_fill_u64(uint64_t* p, uint64_t v, uint64_t n, cudaStream_t st);
 
 // n 32-bit words from mapped pinned host memory to the device with SM

@@ -26,6 +26,14 @@ cudaError_t launch_lz4_decode(const uint8_t* in,
                               uint32_t* status,
                               cudaStream_t st);
 
+// Addresses of one chunk of a batch gathered from several streams.
+struct ChunkRef
+{
+  const uint8_t* in; // chunk_bytes of input (4-byte aligned)
+  uint8_t* out;      // compressed slot (>= the codec bound)
+  uint64_t* size;    // compressed size (written)
+};
+
 struct CodecBatch
 {
   const uint8_t* in;    // first chunk (4-byte aligned)
@@ -48,6 +56,24 @@ struct CodecBatch
   uint64_t id_base;
   uint32_t run_first[kMaxRuns + 1];
   uint32_t run_slot[kMaxRuns];
+
+  // Optional, overriding all of the above addressing: chunk i of the batch
+  // is refs[i] (a device array), so one launch can encode the chunks of
+  // several streams' pools (all of chunk_bytes bytes).
+  const ChunkRef* refs;
+
+  __host__ __device__ const uint8_t* in_at(uint64_t i) const
+  {
+    return refs ? refs[i].in : in + id(i) * in_stride;
+  }
+  __host__ __device__ uint8_t* out_at(uint64_t i) const
+  {
+    return refs ? refs[i].out : out + id(i) * out_stride;
+  }
+  __host__ __device__ uint64_t* size_at(uint64_t i) const
+  {
+    return refs ? refs[i].size : out_sizes + id(i);
+  }
 
   // slot of the i-th chunk of the batch
   __host__ __device__ uint64_t id(uint64_t i) const

@@ -60,7 +60,7 @@ lz4_find_k(CodecBatch b, Seq* seqs, SegMeta* meta, uint32_t regions_per_chunk)
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint64_t chunk = blockIdx.x / regions_per_chunk;
   const uint32_t r0 = (blockIdx.x % regions_per_chunk) * kRegionBytes;
-  const uint8_t* base = b.in + b.id(chunk) * b.in_stride;
+  const uint8_t* base = b.in_at(chunk);
   const uint32_t n = b.chunk_bytes;
   const uint32_t r1 = min(n, r0 + kRegionBytes);
   lz77_stage_region(base, r0, r1, words, threadIdx.x, blockDim.x);
@@ -168,7 +168,7 @@ lz4_plan_k(CodecBatch b, SegMeta* meta)
   if (lane == 0) {
     m[S - 1].final_off = off;
     m[S - 1].final_ll = carry;
-    b.out_sizes[b.id(chunk)] = off + lit_part(carry);
+    *b.size_at(chunk) = off + lit_part(carry);
   }
   __syncwarp();
   // literal field of the run that ends at the final sequence
@@ -221,8 +221,8 @@ lz4_emit_k(CodecBatch b, const Seq* seqs, const SegMeta* meta)
   const uint32_t k = uint32_t(seg % b.segs_per_chunk);
   const SegMeta m = meta[seg];
   const bool last = k + 1 == b.segs_per_chunk;
-  const uint8_t* in = b.in + b.id(chunk) * b.in_stride;
-  uint8_t* out = b.out + b.id(chunk) * b.out_stride;
+  const uint8_t* in = b.in_at(chunk);
+  uint8_t* out = b.out_at(chunk);
   const Seq* s = seqs + seg * kMaxSeqPerSeg;
   const uint32_t s0 = k * kSegBytes;
   const uint32_t s1 = min(b.chunk_bytes, s0 + kSegBytes);

@@ -265,33 +265,7 @@ int plan_stream(const tile_stream_configuration* cfg, StreamPlan* out)
       P.lv[l].lod_nelem *= P.lv[l].shape[P.lod_to_dim[k]];
     P.lod_end[l] = (l ? P.lod_end[l - 1] : 0) + P.lv[l].lod_nelem;
   }
-  if (P.multiscale && P.nlod > 1) {
-    // ends[rank(parent)] = child rank one past the parent's last child
-    // (src/lod/lod_plan.c:105-125, 151-210).
-    P.ends.assign(P.lod_end[P.nlod - 1] - P.lod_end[0], 0);
-    for (int l = 0; l + 1 < P.nlod; ++l) {
-      uint64_t child[LOD_MAX_NDIM], parent[LOD_MAX_NDIM];
-      uint64_t mx = 0;
-      for (int k = 0; k < P.lod_ndim; ++k) {
-        child[k] = P.lv[l].shape[P.lod_to_dim[k]];
-        parent[k] = P.lv[l + 1].shape[P.lod_to_dim[k]];
-        mx = std::max(mx, parent[k]);
-      }
-      const int p = bits_for(mx);
-      uint64_t* seg = P.ends.data() + (P.lod_end[l] - P.lod_end[0]);
-      for (uint64_t j = 0; j < P.lv[l + 1].lod_nelem; ++j) {
-        uint64_t c[LOD_MAX_NDIM], nx[LOD_MAX_NDIM], r = j;
-        for (int k = 0; k < P.lod_ndim; ++k) { // first dim fastest
-          c[k] = r % parent[k];
-          r /= parent[k];
-        }
-        std::memcpy(nx, c, sizeof(uint64_t) * size_t(P.lod_ndim));
-        morton_successor(P.lod_ndim, p, nx);
-        seg[morton_rank(P.lod_ndim, parent, c, 0)] =
-          morton_rank(P.lod_ndim, child, nx, 1);
-      }
-    }
-  }
+  P.n_ends = (P.multiscale && P.nlod > 1) ? P.lod_end[P.nlod - 1] - P.lod_end[0] : 0;
 
   for (int l = 0; l < P.nlod; ++l) {
     level_layout(P.lv[l].layout, P, dims, P.lv[l].shape);
@@ -375,6 +349,43 @@ int plan_stream(const tile_stream_configuration* cfg, StreamPlan* out)
       P.max_cursor *= div_up(dims[d].size, dims[d].chunk_size);
   }
   return 0;
+}
+
+// Morton window ends of every level above 0:
+// ends[rank(parent)] = child rank one past the parent's last child
+// (src/lod/lod_plan.c:105-125, 151-210).  Host work proportional to the
+// pyramid's element count; only the general (Morton-buffer) LOD path reads
+// the table.
+void plan_build_ends(StreamPlan& P)
+{
+  P.ends.clear();
+  if (!P.n_ends)
+    return;
+  {
+    P.ends.assign(P.n_ends, 0);
+    for (int l = 0; l + 1 < P.nlod; ++l) {
+      uint64_t child[LOD_MAX_NDIM], parent[LOD_MAX_NDIM];
+      uint64_t mx = 0;
+      for (int k = 0; k < P.lod_ndim; ++k) {
+        child[k] = P.lv[l].shape[P.lod_to_dim[k]];
+        parent[k] = P.lv[l + 1].shape[P.lod_to_dim[k]];
+        mx = std::max(mx, parent[k]);
+      }
+      const int p = bits_for(mx);
+      uint64_t* seg = P.ends.data() + (P.lod_end[l] - P.lod_end[0]);
+      for (uint64_t j = 0; j < P.lv[l + 1].lod_nelem; ++j) {
+        uint64_t c[LOD_MAX_NDIM], nx[LOD_MAX_NDIM], r = j;
+        for (int k = 0; k < P.lod_ndim; ++k) { // first dim fastest
+          c[k] = r % parent[k];
+          r /= parent[k];
+        }
+        std::memcpy(nx, c, sizeof(uint64_t) * size_t(P.lod_ndim));
+        morton_successor(P.lod_ndim, p, nx);
+        seg[morton_rank(P.lod_ndim, parent, c, 0)] =
+          morton_rank(P.lod_ndim, child, nx, 1);
+      }
+    }
+  }
 }
 
 } // namespace chucky

@@ -63,6 +63,7 @@ struct StreamPlan
   uint64_t chunk_bytes = 0; // chunk_elements * bpe (codec input)
   uint64_t slot_bytes = 0;  // one epoch of every level in the pool
   uint64_t epoch_bytes = 0; // epoch_elements * bpe (input per epoch)
+  uint64_t n_ends = 0;      // entries of the Morton window-end table
 };
 
 // Alignment of chunk strides in the chunk pool (bytes).  Chunk strides only
@@ -75,6 +76,14 @@ uint64_t codec_bound(int codec_id, uint64_t chunk_bytes);
 // 0 on success.  Validation follows src/stream/config.c:144-221.
 int plan_stream(const tile_stream_configuration* cfg, StreamPlan* out);
 
+// Fill P.ends (P.n_ends entries), the Morton window ends the general LOD
+// path reads; plan_stream leaves it empty.
+void plan_build_ends(StreamPlan& P);
+
+// The tiled single-pass pyramid kernel covers this plan (it needs neither
+// the window-end table nor Morton-ordered level buffers).
+bool lod_plan_is_tiled(const StreamPlan& P);
+
 uint64_t morton_rank(int ndim,
                      const uint64_t* shape,
                      const uint64_t* coords,
@@ -84,5 +93,18 @@ uint64_t ravel(int rank,
                const uint64_t* shape,
                const int64_t* strides,
                uint64_t idx);
+
+// Pinned staging slots of a stream.
+constexpr uint64_t kStreamStageSlots = 4;
+
+// Bytes of one pinned staging slot of a stream (it keeps four): a quarter
+// of the configured buffer capacity, 256 KiB to 32 MiB, in whole 4 KiB pages.
+inline uint64_t staging_slot_bytes(uint64_t buffer_capacity_bytes)
+{
+  uint64_t b = buffer_capacity_bytes / 4;
+  b = b < (256ull << 10) ? (256ull << 10) : b;
+  b = b > (32ull << 20) ? (32ull << 20) : b;
+  return (b + 4095) / 4096 * 4096;
+}
 
 } // namespace chucky

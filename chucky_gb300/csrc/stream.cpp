@@ -145,6 +145,14 @@ int Stream::init(const tile_stream_configuration* c, shard_sink* sk)
     CK(cudaMalloc(&d_epoch[i], round_up(P.epoch_bytes, 256) + 256));
     CK(cudaEventRecord(ev_input_free[i], s_comp));
   }
+  stage_bytes = staging_slot_bytes(cfg.buffer_capacity_bytes);
+  stage_small = stage_bytes;
+  for (int i = 0; i < kStageSlots; ++i) {
+    CK(cudaHostAlloc(&h_stage[i], stage_bytes, cudaHostAllocDefault));
+    CK(cudaEventCreateWithFlags(&ev_stage[i], cudaEventDisableTiming));
+  }
+  for (cudaEvent_t* e : { &ev_producer, &ev_consumed })
+    CK(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
   const uint64_t half = uint64_t(P.K) * P.slot_bytes;
   pool_half_bytes = cfg.codec.id == CODEC_NONE ? 0 : half;
   const uint64_t pool_bytes = half + pool_half_bytes;
@@ -214,11 +222,20 @@ int Stream::setup_transpose()
   return 0;
 }
 
+// Whether the tiled single-pass kernel produces every level of this plan
+// from one read of L0 (1..3 LOD dims, the pyramid inside one tile).
+bool lod_plan_is_tiled(const StreamPlan& P)
+{
+  return P.multiscale && P.lod_ndim >= 1 && P.lod_ndim <= 3 && P.nlod <= 16 &&
+         P.nlod - 1 <= lod_tile_levels(P.lod_ndim);
+}
+
 int Stream::setup_lod()
 {
   if (!P.multiscale)
     return 0;
   const int nlod = P.nlod;
+  lod_tiled = lod_plan_is_tiled(P);
   uint64_t total_values = 0, total_accum = 0;
   for (int l = 0; l < nlod; ++l) {
     lod_nelem[l] = P.lv[l].lod_nelem;
@@ -230,36 +247,18 @@ int Stream::setup_lod()
     }
     ends_beg[l] = l >= 1 ? P.lod_end[l - 1] - P.lod_end[0] : 0;
   }
-  CK(cudaMalloc(&d_values, total_values * P.bpe + 16));
   if (P.append_downsample && total_accum)
     CK(cudaMalloc(&d_accum, total_accum * P.bpe + 16));
-  if (!P.ends.empty()) {
-    CK(cudaMalloc(&d_ends, P.ends.size() * 8));
-    CK(cudaMemcpy(d_ends, P.ends.data(), P.ends.size() * 8,
-                  cudaMemcpyHostToDevice));
-  }
 
-  // L0 gather LUT over the row-major epoch (src/cpu/lod.cpp:181-239).
+  // row-major strides of the epoch buffer
   uint64_t stride[HALF_MAX_RANK];
   stride[P.rank - 1] = 1;
   for (int d = P.rank - 2; d >= 0; --d)
     stride[d] = stride[d + 1] * P.lv[0].shape[d + 1];
+  // per slice of the fixed dims: its offset in the epoch buffer and in
+  // each level's chunk slot (both paths)
   {
-    const uint64_t n0 = P.lv[0].lod_nelem;
-    std::vector<uint32_t> lut(n0);
     std::vector<uint64_t> fixed(P.fixed_count);
-    uint64_t shp[LOD_MAX_NDIM];
-    for (int k = 0; k < P.lod_ndim; ++k)
-      shp[k] = P.lv[0].shape[P.lod_to_dim[k]];
-    for (uint64_t g = 0; g < n0; ++g) {
-      uint64_t c[LOD_MAX_NDIM], r = g, off = 0;
-      for (int k = P.lod_ndim - 1; k >= 0; --k) {
-        c[k] = r % shp[k];
-        r /= shp[k];
-        off += c[k] * stride[P.lod_to_dim[k]];
-      }
-      lut[morton_rank(P.lod_ndim, shp, c, 0)] = uint32_t(off);
-    }
     for (uint64_t b = 0; b < P.fixed_count; ++b) {
       uint64_t r = b, off = 0;
       for (int k = P.fixed_ndim - 1; k >= 0; --k) {
@@ -268,35 +267,13 @@ int Stream::setup_lod()
       }
       fixed[b] = off;
     }
-    CK(cudaMalloc(&d_gather_lut, n0 * 4));
     CK(cudaMalloc(&d_gather_fixed, P.fixed_count * 8));
-    CK(cudaMemcpy(d_gather_lut, lut.data(), n0 * 4, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(d_gather_fixed, fixed.data(), P.fixed_count * 8,
                   cudaMemcpyHostToDevice));
   }
-  // Morton -> chunk LUTs per level (src/cpu/lod.cpp:318-352,
-  // src/cpu/pipeline.c:373-398).
   for (int l = 0; l < nlod; ++l) {
     const tile_stream_layout& L = P.lv[l].layout;
-    const uint64_t n = P.lv[l].lod_nelem;
-    std::vector<uint32_t> lut(n);
     std::vector<uint64_t> fixed(P.fixed_count);
-    uint64_t shp[LOD_MAX_NDIM];
-    for (int k = 0; k < P.lod_ndim; ++k)
-      shp[k] = P.lv[l].shape[P.lod_to_dim[k]];
-    for (uint64_t g = 0; g < n; ++g) {
-      uint64_t c[LOD_MAX_NDIM], r = g;
-      int64_t off = 0;
-      for (int k = P.lod_ndim - 1; k >= 0; --k) {
-        c[k] = r % shp[k];
-        r /= shp[k];
-        const int d = P.lod_to_dim[k];
-        const uint64_t cs = L.lifted_shape[2 * d + 1];
-        off += int64_t(c[k] / cs) * L.lifted_strides[2 * d] +
-               int64_t(c[k] % cs) * L.lifted_strides[2 * d + 1];
-      }
-      lut[morton_rank(P.lod_ndim, shp, c, 0)] = uint32_t(off);
-    }
     for (uint64_t b = 0; b < P.fixed_count; ++b) {
       uint64_t r = b;
       int64_t off = 0;
@@ -310,17 +287,67 @@ int Stream::setup_lod()
       }
       fixed[b] = uint64_t(off) + P.lv[l].chunk_offset * L.chunk_stride;
     }
-    CK(cudaMalloc(&d_chunk_lut[l], n * 4));
     CK(cudaMalloc(&d_chunk_fixed[l], P.fixed_count * 8));
-    CK(cudaMemcpy(d_chunk_lut[l], lut.data(), n * 4, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(d_chunk_fixed[l], fixed.data(), P.fixed_count * 8,
                   cudaMemcpyHostToDevice));
   }
-  // The tiled kernel produces every level from one read of L0 when the
-  // LOD dims are 1..3 and the pyramid fits inside one tile.
-  if (P.lod_ndim >= 1 && P.lod_ndim <= 3 && P.nlod <= 16 &&
-      P.nlod - 1 <= lod_tile_levels(P.lod_ndim)) {
-    lod_tiled = true;
+
+  if (!lod_tiled) {
+    // The general path: Morton-ordered level buffers, window ends and the
+    // L0 gather / per-level scatter LUTs (host work and memory in
+    // proportion to the pyramid's element count).
+    CK(cudaMalloc(&d_values, total_values * P.bpe + 16));
+    plan_build_ends(P);
+    if (!P.ends.empty()) {
+      CK(cudaMalloc(&d_ends, P.ends.size() * 8));
+      CK(cudaMemcpy(d_ends, P.ends.data(), P.ends.size() * 8,
+                    cudaMemcpyHostToDevice));
+    }
+    // L0 gather LUT over the row-major epoch (src/cpu/lod.cpp:181-239).
+    {
+      const uint64_t n0 = P.lv[0].lod_nelem;
+      std::vector<uint32_t> lut(n0);
+      uint64_t shp[LOD_MAX_NDIM];
+      for (int k = 0; k < P.lod_ndim; ++k)
+        shp[k] = P.lv[0].shape[P.lod_to_dim[k]];
+      for (uint64_t g = 0; g < n0; ++g) {
+        uint64_t c[LOD_MAX_NDIM], r = g, off = 0;
+        for (int k = P.lod_ndim - 1; k >= 0; --k) {
+          c[k] = r % shp[k];
+          r /= shp[k];
+          off += c[k] * stride[P.lod_to_dim[k]];
+        }
+        lut[morton_rank(P.lod_ndim, shp, c, 0)] = uint32_t(off);
+      }
+      CK(cudaMalloc(&d_gather_lut, n0 * 4));
+      CK(cudaMemcpy(d_gather_lut, lut.data(), n0 * 4, cudaMemcpyHostToDevice));
+    }
+    // Morton -> chunk LUTs per level (src/cpu/lod.cpp:318-352,
+    // src/cpu/pipeline.c:373-398).
+    for (int l = 0; l < nlod; ++l) {
+      const tile_stream_layout& L = P.lv[l].layout;
+      const uint64_t n = P.lv[l].lod_nelem;
+      std::vector<uint32_t> lut(n);
+      uint64_t shp[LOD_MAX_NDIM];
+      for (int k = 0; k < P.lod_ndim; ++k)
+        shp[k] = P.lv[l].shape[P.lod_to_dim[k]];
+      for (uint64_t g = 0; g < n; ++g) {
+        uint64_t c[LOD_MAX_NDIM], r = g;
+        int64_t off = 0;
+        for (int k = P.lod_ndim - 1; k >= 0; --k) {
+          c[k] = r % shp[k];
+          r /= shp[k];
+          const int d = P.lod_to_dim[k];
+          const uint64_t cs = L.lifted_shape[2 * d + 1];
+          off += int64_t(c[k] / cs) * L.lifted_strides[2 * d] +
+                 int64_t(c[k] % cs) * L.lifted_strides[2 * d + 1];
+        }
+        lut[morton_rank(P.lod_ndim, shp, c, 0)] = uint32_t(off);
+      }
+      CK(cudaMalloc(&d_chunk_lut[l], n * 4));
+      CK(cudaMemcpy(d_chunk_lut[l], lut.data(), n * 4, cudaMemcpyHostToDevice));
+    }
+  } else {
     LodTileArgs& t = tile;
     t.dtype = cfg.dtype;
     t.method = cfg.reduce_method;
@@ -457,6 +484,18 @@ void Stream::release()
   if (s_copy)
     cudaStreamSynchronize(s_copy);
   codec_release();
+  for (int i = 0; i < kStageSlots; ++i) {
+    cudaFreeHost(h_stage[i]);
+    h_stage[i] = nullptr;
+    if (ev_stage[i])
+      cudaEventDestroy(ev_stage[i]);
+    ev_stage[i] = nullptr;
+  }
+  for (cudaEvent_t* e : { &ev_producer, &ev_consumed })
+    if (*e) {
+      cudaEventDestroy(*e);
+      *e = nullptr;
+    }
   for (int i = 0; i < 2; ++i) {
     cudaFree(d_epoch[i]);
     if (ev_input_ready[i])
@@ -547,6 +586,8 @@ int Stream::claim_pool()
 int Stream::run_epoch(uint64_t present)
 {
   const int b = in_buf;
+  if (stage_issue())
+    return 1;
   CK(cudaEventRecord(ev_input_ready[b], s_copy));
   CK(cudaStreamWaitEvent(s_comp, ev_input_ready[b], 0));
   if (present < layout.epoch_elements) // partial final epoch: fill value 0
@@ -701,12 +742,34 @@ int Stream::kick_batch(uint32_t n_epochs, const uint32_t* epoch_masks)
     // the aggregation that read this compressed slot two batches ago must
     // be done before the encoders overwrite it
     CK(cudaStreamWaitEvent(se, ev_agg_done[si], 0));
-    if (timed_begin(se, &metrics.compress, double(n * P.chunk_bytes), 0))
-      return 1;
-    if (codec_compress(comp, n, d_ids, rp, d_comp[si], d_sizes[si], codec_state[si], se))
-      return 1;
-    if (timed_end(se))
-      return 1;
+    if (engine) {
+      // the shared engine encodes this batch with other streams' batches
+      EncodeJob& J = job[si];
+      J = EncodeJob{};
+      J.codec = cfg.codec.id;
+      J.level = cfg.codec.level;
+      J.chunk_bytes = uint32_t(P.chunk_bytes);
+      J.pool = comp;
+      J.in_stride = layout.chunk_stride * P.bpe;
+      J.slots = ids;
+      J.n = n;
+      J.out = d_comp[si];
+      J.out_stride = comp_stride;
+      J.sizes = d_sizes[si];
+      J.ready = ev_pool_ready;
+      J.out_free = ev_agg_done[si];
+      J.done = ev_engine_done[si];
+      if (engine->run(J))
+        return 1;
+      CK(cudaStreamWaitEvent(se, ev_engine_done[si], 0));
+    } else {
+      if (timed_begin(se, &metrics.compress, double(n * P.chunk_bytes), 0))
+        return 1;
+      if (codec_compress(comp, n, d_ids, rp, d_comp[si], d_sizes[si], codec_state[si], se))
+        return 1;
+      if (timed_end(se))
+        return 1;
+    }
     comp = d_comp[si];
   }
   AggBatch ab{};
@@ -781,7 +844,11 @@ int Stream::kick_batch(uint32_t n_epochs, const uint32_t* epoch_masks)
   if (timed_begin(sa, &metrics.aggregate, 0, 0))
     return 1;
   CK(launch_aggregate(ab, d_agg_scratch + si * agg_scratch_slot, sa));
-  // to the host: the expected bytes now, the rest (if any) at delivery
+  // to the host: the expected bytes by the copy engine, the rest (if the
+  // batch is larger: the first batch, or a less compressible one) by a
+  // kernel that reads the total on the device -- no host wait either way
+  TailCopies tails{};
+  uint64_t tail_max = 0;
   for (int k = 0; k < S.n_levels; ++k) {
     DeliverySlot::Level& D = S.lv[S.level_of[k]];
     if (!D.d_data)
@@ -789,7 +856,16 @@ int Stream::kick_batch(uint32_t n_epochs, const uint32_t* epoch_masks)
     D.copied = std::min(agg_estimate[S.level_of[k]], D.data_cap);
     if (D.copied)
       CK(cudaMemcpyAsync(D.data, D.d_data, D.copied, cudaMemcpyDeviceToHost, sa));
+    if (D.copied < D.data_cap) {
+      TailCopy& t = tails.lv[tails.n++];
+      t.dst = D.data;
+      t.src = D.d_data;
+      t.total = D.offsets + D.positions; // mapped: written by the aggregation
+      t.start = D.copied;
+      tail_max = std::max(tail_max, D.data_cap - D.copied);
+    }
   }
+  CK(launch_tail_copy(tails, tail_max, sa));
   if (timed_end(sa))
     return 1;
   CK(cudaEventRecord(ev_agg_done[si], sa));
@@ -819,9 +895,7 @@ int Stream::deliver(int si)
     if (!D.d_data)
       continue;
     const uint64_t total = D.offsets[D.positions];
-    if (total > D.copied) // more than expected: copy the rest now
-      CK(cudaMemcpy(D.data + D.copied, D.d_data + D.copied, total - D.copied,
-                    cudaMemcpyDeviceToHost));
+    // (bytes beyond the expected size arrived by the tail kernel)
     agg_estimate[l] = total + total / 32 + (16u << 10);
   }
   const double t0 = now_ms();
@@ -960,17 +1034,97 @@ int Stream::batch_boundary()
 // writer vtable
 // ---------------------------------------------------------------------------
 
+// Issue the copy of the staging slot being filled (if it holds anything).
+int Stream::stage_issue()
+{
+  if (!stage_fill)
+    return 0;
+  CK(cudaMemcpyAsync(stage_dst, h_stage[stage_cur], stage_fill,
+                     cudaMemcpyHostToDevice, s_copy));
+  CK(cudaEventRecord(ev_stage[stage_cur], s_copy));
+  stage_used[stage_cur] = true;
+  stage_cur = (stage_cur + 1) % kStageSlots;
+  stage_fill = 0;
+  return 0;
+}
+
+// Copy host bytes through the staging ring to `dst` in an epoch buffer.
+int Stream::stage_copy(uint8_t* dst, const uint8_t* src, uint64_t bytes)
+{
+  while (bytes) {
+    if (stage_fill && dst != stage_dst + stage_fill && stage_issue())
+      return 1;
+    if (!stage_fill) {
+      if (stage_used[stage_cur]) // its previous copy must have read it
+        CK(cudaEventSynchronize(ev_stage[stage_cur]));
+      stage_dst = dst;
+    }
+    const uint64_t n = std::min(bytes, stage_bytes - stage_fill);
+    std::memcpy(h_stage[stage_cur] + stage_fill, src, n);
+    stage_fill += n;
+    dst += n;
+    src += n;
+    bytes -= n;
+    if (stage_fill == stage_bytes && stage_issue())
+      return 1;
+  }
+  return 0;
+}
+
+namespace {
+
+enum class Source
+{
+  staged, // pageable, or small pinned: through the staging ring
+  direct, // large pinned host memory: copied from the caller, waited for
+  device, // device memory: copied on the device, waited for
+};
+
+Source classify(const void* p, uint64_t bytes, uint64_t small)
+{
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return Source::staged;
+  }
+  if (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged)
+    return Source::device;
+  if (a.type == cudaMemoryTypeHost && bytes > small)
+    return Source::direct;
+  return Source::staged;
+}
+
+} // namespace
+
 writer_result Stream::append(slice in)
+{
+  return append_async(in, nullptr);
+}
+
+writer_result Stream::append_async(slice in, cudaStream_t producer)
 {
   if (flushed)
     return writer_finished_at(in.beg, in.end);
   const uint8_t* src = static_cast<const uint8_t*>(in.beg);
   const uint8_t* end = static_cast<const uint8_t*>(in.end);
+  if (src >= end)
+    return writer_result{ 0, { src, end } };
   const uint64_t ee = layout.epoch_elements;
   const double t0 = now_ms();
+  const Source kind = classify(src, uint64_t(end - src), stage_small);
+  if (producer) {
+    // stream-ordered hand-off of device memory only
+    if (kind != Source::device)
+      return writer_error_at(src, end);
+    if (cudaEventRecord(ev_producer, producer) != cudaSuccess ||
+        cudaStreamWaitEvent(s_copy, ev_producer, 0) != cudaSuccess)
+      return writer_error_at(src, end);
+  }
   uint64_t copied = 0;
+  double memcpy_ms = 0;
   while (src < end) {
     if (max_cursor > 0 && cursor >= max_cursor) {
+      // every copy out of the caller's buffer has finished after this
       cudaStreamSynchronize(s_copy);
       if (flush_all())
         return writer_error_at(src, end);
@@ -985,9 +1139,16 @@ writer_result Stream::append(slice in)
     if (in_fill == 0 &&
         cudaStreamWaitEvent(s_copy, ev_input_free[in_buf], 0) != cudaSuccess)
       return writer_error_at(src, end);
-    if (cudaMemcpyAsync(d_epoch[in_buf] + in_fill * P.bpe, src, n * P.bpe,
-                        cudaMemcpyDefault, s_copy) != cudaSuccess)
+    uint8_t* dst = d_epoch[in_buf] + in_fill * P.bpe;
+    if (kind == Source::staged) {
+      const double m0 = now_ms();
+      if (stage_copy(dst, src, n * P.bpe))
+        return writer_error_at(src, end);
+      memcpy_ms += now_ms() - m0;
+    } else if (cudaMemcpyAsync(dst, src, n * P.bpe, cudaMemcpyDefault, s_copy) !=
+               cudaSuccess) {
       return writer_error_at(src, end);
+    }
     copied += n * P.bpe;
     in_fill += n;
     cursor += n;
@@ -999,12 +1160,22 @@ writer_result Stream::append(slice in)
         return writer_error_at(src, end);
     }
   }
-  // the caller's buffer is only borrowed for the duration of the call
-  if (cudaStreamSynchronize(s_copy) != cudaSuccess)
-    return writer_error_at(src, end);
-  if (copied)
-    add_metric(metrics.h2d, float(now_ms() - t0), double(copied),
-               double(copied));
+  if (producer) {
+    // the producer's later work (e.g. overwriting its buffer) waits for
+    // the copies out of it
+    if (cudaEventRecord(ev_consumed, s_copy) != cudaSuccess ||
+        cudaStreamWaitEvent(producer, ev_consumed, 0) != cudaSuccess)
+      return writer_error_at(src, end);
+  } else if (kind != Source::staged) {
+    // the caller's buffer is only borrowed for the duration of the call
+    if (cudaStreamSynchronize(s_copy) != cudaSuccess)
+      return writer_error_at(src, end);
+  }
+  if (copied) {
+    add_metric(metrics.h2d, float(now_ms() - t0), double(copied), double(copied));
+    if (memcpy_ms > 0)
+      add_metric(metrics.memcpy, float(memcpy_ms), double(copied), double(copied));
+  }
   return writer_result{ 0, { src, end } };
 }
 
@@ -1097,9 +1268,11 @@ vt_flush(writer* w)
   return reinterpret_cast<tile_stream_gpu*>(w)->impl.flush();
 }
 
-extern "C" tile_stream_gpu*
-tile_stream_gpu_create(const tile_stream_configuration* config,
-                       shard_sink* sink)
+namespace chucky {
+
+tile_stream_gpu* create_stream(const tile_stream_configuration* config,
+                               shard_sink* sink,
+                               Engine* engine)
 {
   if (!config || !sink || !sink->open)
     return nullptr;
@@ -1108,12 +1281,30 @@ tile_stream_gpu_create(const tile_stream_configuration* config,
     return nullptr;
   s->w.append = vt_append;
   s->w.flush = vt_flush;
+  s->impl.engine = engine;
   if (s->impl.init(config, sink)) {
     s->impl.release();
     delete s;
     return nullptr;
   }
   return s;
+}
+
+} // namespace chucky
+
+extern "C" tile_stream_gpu*
+tile_stream_gpu_create(const tile_stream_configuration* config,
+                       shard_sink* sink)
+{
+  return chucky::create_stream(config, sink, nullptr);
+}
+
+extern "C" writer_result
+tile_stream_gpu_append_device(tile_stream_gpu* s, slice data, void* cuda_stream)
+{
+  if (!s || !cuda_stream)
+    return writer_error_at(data.beg, data.end);
+  return s->impl.append_async(data, static_cast<cudaStream_t>(cuda_stream));
 }
 
 extern "C" void
@@ -1186,6 +1377,9 @@ tile_stream_gpu_restart(tile_stream_gpu* s, shard_sink* sink)
     I.sink = sink;
   I.cursor = 0;
   I.flushed = 0;
+  I.stage_fill = 0;
+  for (bool& u : I.stage_used)
+    u = false;
   I.pending_epoch_ms.clear();
   I.accumulated = 0;
   I.in_buf = 0;

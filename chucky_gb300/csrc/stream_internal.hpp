@@ -1,6 +1,7 @@
 // Internal state of one GPU stream (not part of the C ABI).
 #pragma once
 
+#include "engine.hpp"
 #include "kernels.hpp"
 #include "plan.hpp"
 #include "stream.gpu.h"
@@ -62,6 +63,26 @@ struct Stream
   int in_buf = 0;
   uint64_t in_fill = 0;
 
+  // Pinned staging ring for appends of pageable memory and small appends of
+  // any host memory: `append` copies the caller's bytes into a slot with the
+  // CPU and returns; the slot's copy to the epoch buffer runs on the copy
+  // stream.  Consecutive appends that land next to each other in the epoch
+  // buffer share a slot, whose copy is issued when it is full, when the
+  // epoch is complete, or at the flush.  A slot is written again only after
+  // its copy has finished (its event).
+  static constexpr int kStageSlots = int(kStreamStageSlots);
+  uint8_t* h_stage[kStageSlots] = {};
+  cudaEvent_t ev_stage[kStageSlots] = {};
+  bool stage_used[kStageSlots] = {};
+  uint64_t stage_bytes = 0;  // bytes per slot
+  int stage_cur = 0;         // slot being filled
+  uint64_t stage_fill = 0;   // bytes in it not yet issued
+  uint8_t* stage_dst = nullptr; // device destination of its first byte
+  // appends of pinned host memory up to this size go through the ring
+  uint64_t stage_small = 0;
+  // stream-ordered appends of device memory (append_async)
+  cudaEvent_t ev_producer = nullptr, ev_consumed = nullptr;
+
   // chunk pool / compression.  With a codec the pool has two halves, one
   // per delivery slot: the LOD of the next batch fills one half while the
   // encoders of the previous one read the other.  Each slot has its own
@@ -80,6 +101,12 @@ struct Stream
   uint64_t wave_chunks = 0; // chunks per encoder launch
   uint32_t* h_chunk_ids[2] = {};   // pinned staging of the encode list
   uint32_t* d_chunk_ids[2] = {};
+  // With a shared encoder engine (the served form) the stream has no
+  // encoder scratch: each batch's chunks go to the engine as a job, whose
+  // encoders signal ev_engine_done of the delivery slot.
+  Engine* engine = nullptr;
+  EncodeJob job[2];
+  cudaEvent_t ev_engine_done[2] = {};
 
   // transpose
   uint64_t* d_row_off = nullptr;
@@ -170,7 +197,13 @@ struct Stream
   int finalize_level(int l);
   int flush_all();
   writer_result append(slice in);
+  // Device memory appended in stream order with `producer` (a cudaStream_t
+  // of the caller): the copies wait for the producer's work so far, and the
+  // producer's later work waits for the copies; the host does not wait.
+  writer_result append_async(slice in, cudaStream_t producer);
   writer_result flush();
+  int stage_issue();
+  int stage_copy(uint8_t* dst, const uint8_t* src, uint64_t bytes);
 
   int codec_init();
   int codec_compress(const uint8_t* pool,

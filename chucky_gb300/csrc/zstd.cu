@@ -198,7 +198,7 @@ zstd_find_k(CodecBatch b,
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint64_t chunk = blockIdx.x / regions_per_chunk;
   const uint32_t r0 = (blockIdx.x % regions_per_chunk) * kRegionBytes;
-  const uint8_t* base = b.in + b.id(chunk) * b.in_stride;
+  const uint8_t* base = b.in_at(chunk);
   const uint32_t r1 = min(b.chunk_bytes, r0 + kRegionBytes);
   lz77_stage_region(base, r0, r1, words, threadIdx.x, blockDim.x);
   const uint32_t s0 = r0 + w * kSegBytes;
@@ -1188,7 +1188,7 @@ zstd_block_k(CodecBatch b,
   const uint64_t blk = blockIdx.x;
   const uint64_t chunk = blk / blocks_per_chunk;
   const uint32_t bi = uint32_t(blk % blocks_per_chunk);
-  const uint8_t* in = b.in + b.id(chunk) * b.in_stride;
+  const uint8_t* in = b.in_at(chunk);
   const uint32_t b0 = bi * kBlockBytes;
   const uint32_t b1 = min(b.chunk_bytes, b0 + kBlockBytes);
   const uint32_t bsize = b1 - b0;
@@ -1657,7 +1657,7 @@ zstd_frame_k(CodecBatch b,
   const uint64_t blk = blockIdx.x;
   const uint64_t chunk = blk / blocks_per_chunk;
   const uint32_t k = uint32_t(blk % blocks_per_chunk);
-  uint8_t* out = b.out + b.id(chunk) * b.out_stride;
+  uint8_t* out = b.out_at(chunk);
   const uint32_t n = b.chunk_bytes;
   const uint32_t* sizes = block_sizes + chunk * blocks_per_chunk;
   if (threadIdx.x < 32) {
@@ -1684,7 +1684,7 @@ zstd_frame_k(CodecBatch b,
         }
       }
       if (k + 1 == blocks_per_chunk)
-        b.out_sizes[b.id(chunk)] = h + acc + sizes[k];
+        *b.size_at(chunk) = h + acc + sizes[k];
     }
   }
   __syncthreads();

@@ -23,6 +23,22 @@ extern "C"
   int tile_stream_gpu_restart(struct tile_stream_gpu* s,
                               struct shard_sink* sink);
 
+  /* Append device memory in stream order with the caller's CUDA stream
+   * `cuda_stream` (a cudaStream_t, not NULL): the copies out of `data` wait
+   * for the work queued on `cuda_stream` so far (so a kernel of the caller
+   * may still be producing the frame), and work the caller queues on
+   * `cuda_stream` afterwards waits for those copies (so the caller may
+   * reuse its buffer in stream order).  The host does not wait for either.
+   * Otherwise as writer_append (result codes, `rest`, bounded capacity).
+   * `data` must be device or managed memory; host memory is rejected with
+   * writer_error_fail.  The reference has no counterpart; its devlog lists
+   * this hand-off as a TODO (docs/devlog.md:9).  Plain writer_append
+   * accepts device pointers too, but waits for its copies before it
+   * returns. */
+  struct writer_result tile_stream_gpu_append_device(struct tile_stream_gpu* s,
+                                                     struct slice data,
+                                                     void* cuda_stream);
+
   /* Append-to-delivered latency of every epoch delivered so far, in ms:
    * from the append call that completed the epoch's input to the end of
    * the sink writes of the batch holding it.  Writes up to `cap` values to
@@ -68,8 +84,8 @@ extern "C"
    * stream).  The output is byte-identical to what a tile_stream_gpu with
    * CODEC_LZ4_NON_STANDARD writes for the same chunk bytes.
    *
-   * All calls on a device share the one scratch array: calls ordered on one
-   * CUDA stream are safe, calls that may overlap (other streams, other
+   * All calls in a context share its one scratch array: calls ordered on
+   * one CUDA stream are safe, calls that may overlap (other streams, other
    * threads) race.  No part of the array needs to start at zero.
    *
    * Returns 0 on success, 1 for invalid arguments, 2 when the request
@@ -83,6 +99,38 @@ extern "C"
                                       size_t out_stride,
                                       uint64_t* d_sizes,
                                       void* cuda_stream);
+
+  /* Batched chunk encoding on the device, the stream's own encoders as a
+   * library call (the batch counterpart of the reference's codec_compress,
+   * src/gpu/compress.cu:284-369, which calls nvcomp).
+   *
+   * chucky_encode_bound: worst-case encoded size of one chunk (0 for a
+   * codec other than CODEC_LZ4_NON_STANDARD / CODEC_ZSTD).
+   * chucky_encode_scratch_bytes: device scratch chucky_encode_chunks needs.
+   * chucky_encode_chunks: encodes `n_chunks` chunks of `chunk_bytes`, chunk
+   * i at d_chunks + i * in_stride (device memory, 4-byte aligned, the 256
+   * bytes after the last chunk readable), into raw LZ4 blocks or zstd
+   * frames at d_out + i * out_stride (out_stride >= the bound), sizes at
+   * d_sizes[i], asynchronously on `cuda_stream` (a cudaStream_t; NULL for
+   * the default stream), using `d_scratch` (not shared with a call that may
+   * overlap).  The output equals what a tile_stream_gpu with that codec
+   * writes for the same chunk bytes.  Returns 0, 1 for invalid arguments,
+   * 3 for a CUDA error. */
+  size_t chucky_encode_bound(int codec_id, size_t chunk_bytes);
+  size_t chucky_encode_scratch_bytes(int codec_id, size_t chunk_bytes,
+                                     size_t n_chunks);
+  int chucky_encode_chunks(int codec_id,
+                           int level,
+                           const void* d_chunks,
+                           size_t chunk_bytes,
+                           size_t in_stride,
+                           size_t n_chunks,
+                           void* d_out,
+                           size_t out_stride,
+                           uint64_t* d_sizes,
+                           void* d_scratch,
+                           size_t scratch_bytes,
+                           void* cuda_stream);
 
   /* Decode raw LZ4 blocks (CODEC_LZ4_NON_STANDARD chunks) on the device,
    * for on-device verification and readback; no counterpart in the

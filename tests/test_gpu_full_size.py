@@ -8,9 +8,13 @@ shard indexes and their crc32c are valid.
   * the 256^3 u16 cube with LZ4 and no pyramid;
   * 2304 x 4096 u16 sensor frames, chunk 32 x 256 x 256, 5-level max
     pyramid with dim-0 downsampling: 64 frames (two epochs, so level 1 is
-    folded and emitted), zstd-1 and LZ4;
-  * one rank-5 (t, c, z, y, x) f16 array 1 x 3 x 128 x 512 x 512 with
-    zero / constant / random chunks, min_sup pyramid, zstd-1.
+    folded and emitted), zstd-1 and LZ4; and 512 frames (16 epochs: every
+    level 1..4 folds and emits in steady state, level 4 once per 16
+    epochs), zstd-1, appended frame by frame;
+  * the batched rank-5 (t, c, z, y, x) arrays t x 3 x 128 x 512 x 512 in
+    all five dtypes (u8 t=8, i16 / u16 / f16 t=4, f32 t=2: 768 MiB each)
+    with zero / constant / random chunks, max_sup / min_sup pyramid,
+    zstd-1.
 Inputs are the benchmark's own seeded generators."""
 import os
 import sys
@@ -68,8 +72,27 @@ def test_sensor_frames_two_epochs(codec):
     assert comp < raw
 
 
-def test_batched_rank5_f16():
+def test_sensor_frames_sixteen_epochs():
     import torch
-    arr = bench.batched_array("f16", 1, torch.device("cuda")).cpu().numpy()
-    comp, raw = _check(bench.batched_config("f16", 1, "min_sup"), arr, "zstd")
+    frames = bench.sensor_frames(512, torch.device("cuda")).cpu().numpy().view("<u2")
+    cfg = bench.sensor_config("zstd", "max")
+    frame_bytes = 2304 * 4096 * 2
+    pieces = list(range(frame_bytes, frames.nbytes, frame_bytes))
+    got, _ = H.run_gpu(cfg, frames, pieces)
+    want, _ = H.run_oracle(_raw_config(cfg), frames, quirks=False)
+    checked, comp, raw = H.compare_decoded(cfg, got, want, "zstd")
+    levels = {k[0] for k in want}
+    assert levels == {0, 1, 2, 3, 4}, levels
+    # level l emits 16 / 2^l epochs of ceil(9 / 2^l) x ceil(16 / 2^l)
+    # chunks of 256 x 256: 16*144 + 8*40 + 4*12 + 2*4 + 1*1, all checked
+    assert checked == 2681
+    assert comp < raw
+
+
+@pytest.mark.parametrize("dtype,t,reduce", bench.BATCHED_DTYPES,
+                         ids=[d[0] for d in bench.BATCHED_DTYPES])
+def test_batched_rank5(dtype, t, reduce):
+    import torch
+    arr = bench.batched_array(dtype, t, torch.device("cuda")).cpu().numpy()
+    comp, raw = _check(bench.batched_config(dtype, t, reduce), arr, "zstd")
     assert comp * 2 < raw  # half the chunks are zero, a quarter constant

@@ -1,12 +1,16 @@
-"""Served form: a request's shards are the same whether it runs alone or
-concurrently with others on resident, restarted streams.
+"""Served form through the C server (include/chucky_serve.h): a request's
+shards are the same whether it runs alone or concurrently with others.
 
-Each request writes into its own memory sink.  The requests run first one at
-a time (run_plain) and then all together with Poisson-paced appends and a
-memory budget that admits only some of them at once (run_served), which
-also exercises stream reuse through tile_stream_gpu_restart.  Every shard
-must match byte for byte, and every chunk must decode to the oracle's raw
-chunk bytes.
+Requests of the four served shapes -- the 256^3 u16 cube appended frame by
+frame, 2304 x 4096 u16 sensor frames, 512^2 x 64 f32 stacks, 1024^2 u8
+frames (shortened to one or two epochs each) -- with LZ4 / zstd and half of
+them with a mean pyramid, each writing into its own memory sink.  They run
+first one at a time (max_streams 1, every stream encoding on its own), then
+all together with Poisson-paced appends, encoders batched across streams by
+the shared engine, and a memory budget that admits only some of them at once
+(admission waits, restarted streams).  Every shard must match byte for
+byte, and every chunk of one request per shape must decode to the oracle's
+raw chunk bytes.
 """
 import numpy as np
 import pytest
@@ -15,84 +19,82 @@ from harness import MemSink, compare_decoded, run_oracle
 
 pytestmark = pytest.mark.gpu
 
-D = dict
+FRAMES = {"cube": 256, "sensor": 32, "stack": 2, "frames8": 64}
 
 
-def _requests(torch, sinks):
+def _requests(sinks):
     from chucky_gb300 import serve
-    rng = np.random.default_rng(21)
-    specs = [
-        # (dims, kwargs, frame bytes, frames)
-        ([D(size=64, chunk=16, cps=2, name="z", downsample=1),
-          D(size=64, chunk=16, cps=2, name="y", downsample=1),
-          D(size=64, chunk=16, cps=2, name="x", downsample=1)],
-         dict(dtype="u16", codec="lz4", level=1, reduce="mean", append_reduce="mean",
-              max_nlod=3, epochs_per_batch=2), 64 * 64 * 2, 64),
-        ([D(size=0, chunk=4, cps=1, name="t"),
-          D(size=96, chunk=32, cps=2, name="y", downsample=1),
-          D(size=128, chunk=32, cps=2, name="x", downsample=1)],
-         dict(dtype="u16", codec="zstd", level=1, reduce="max", append_reduce="max",
-              max_nlod=3, epochs_per_batch=2), 96 * 128 * 2, 22),
-        ([D(size=0, chunk=8, cps=1, name="t"),
-          D(size=128, chunk=64, cps=2, name="y"),
-          D(size=128, chunk=64, cps=2, name="x")],
-         dict(dtype="u8", codec="lz4", level=1), 128 * 128, 40),
-        ([D(size=0, chunk=1, cps=1, name="t"),
-          D(size=16, chunk=16, cps=1, name="z"),
-          D(size=64, chunk=32, cps=2, name="y", downsample=1),
-          D(size=64, chunk=32, cps=2, name="x", downsample=1)],
-         dict(dtype="f32", codec="zstd", level=1, reduce="mean", append_reduce="mean",
-              max_nlod=2), 16 * 64 * 64 * 4, 5),
-    ]
-    reqs, raw = [], []
-    for i, (dims, kw, frame, frames) in enumerate(specs * 2):
-        n = frame * frames
-        if kw["dtype"] == "f32":
-            x = rng.normal(0, 1, size=n // 4).astype("<f4").view(np.uint8)
-        else:
-            x = (rng.integers(0, 32, size=n, dtype=np.uint8) | (np.arange(n) % 7 == 0))
-            x = x.astype(np.uint8)
-        raw.append(x)
-        reqs.append(serve.Request(name=f"r{i}", cfg_kwargs=dict(kw), dims=dims,
-                                  data=torch.from_numpy(x), frame_bytes=frame,
-                                  arrival_s=0.002 * i, mean_gap_s=0.0005,
-                                  sink=sinks[i].base))
-    return reqs, raw
-
-
-def _shards(sinks):
-    return [s.shards() for s in sinks]
+    reqs = serve.c5_requests(seed=21, n=len(sinks), mean_gap_s=0.0003,
+                             arrival_gap_s=0.002, frames=FRAMES)
+    for r, s in zip(reqs, sinks):
+        r.sink = s.base
+    return reqs
 
 
 def test_served_matches_alone():
-    torch = pytest.importorskip("torch")
     from chucky_gb300 import serve
-    alone_sinks = [MemSink() for _ in range(8)]
-    mix_sinks = [MemSink() for _ in range(8)]
+    n = 8
+    alone_sinks = [MemSink() for _ in range(n)]
+    mix_sinks = [MemSink() for _ in range(n)]
     try:
-        reqs, raw = _requests(torch, alone_sinks)
-        serve.run_plain(reqs)
-        alone = _shards(alone_sinks)
-        reqs, _ = _requests(torch, mix_sinks)
+        reqs = _requests(alone_sinks)
+        serve.run_plain(reqs, warmup=False)
+        alone = [s.shards() for s in alone_sinks]
+        reqs = _requests(mix_sinks)
         # a budget for about three requests at a time: admission waits and
         # restarted (reused) streams both happen
-        budget = 3 * max(serve.memory_estimate(serve.load(), r) for r in reqs)
-        out = serve.run_served(reqs, hbm_budget=budget, max_streams=4)
-        assert out["epochs"] > 0
-        mixed = _shards(mix_sinks)
+        budget = 3 * max(serve.memory_estimate(r) for r in reqs)
+        st = serve.run_served(reqs, hbm_budget=budget, max_streams=4, paced=True,
+                              warmup=False)
+        assert st["requests"] == n and st["epochs"] > 0
+        assert st["engine_rounds"] > 0 and st["engine_jobs"] >= st["engine_rounds"]
+        assert st["streams_reused"] + st["streams_created"] == n
+        mixed = [s.shards() for s in mix_sinks]
         for i, (a, m) in enumerate(zip(alone, mixed)):
-            assert a.keys() == m.keys(), f"request {i}: shard sets differ"
+            assert a.keys() == m.keys(), f"request {reqs[i].name}: shard sets differ"
             for k in a:
-                assert a[k] == m[k], f"request {i} shard {k} differs"
-        # and the data itself: every chunk decodes to the oracle's bytes
-        for i in range(4):
-            raw_kw = dict(reqs[i].cfg_kwargs, codec="none")
-            cfg = serve.Request(name="raw", cfg_kwargs=raw_kw, dims=reqs[i].dims,
+                assert a[k] == m[k], f"request {reqs[i].name} shard {k} differs"
+        # the data itself: every chunk decodes to the oracle's bytes (one
+        # request of each shape)
+        seen = set()
+        for i, r in enumerate(reqs):
+            kind = r.name.split(":")[1]
+            if kind in seen:
+                continue
+            seen.add(kind)
+            raw_kw = dict(r.cfg_kwargs, codec="none")
+            cfg = serve.Request(name="raw", cfg_kwargs=raw_kw, dims=r.dims,
                                 data=None, frame_bytes=0).config()
-            shards_raw, _ = run_oracle(cfg, raw[i], quirks=False)
-            n, _, _ = compare_decoded(reqs[i].config(), mixed[i], shards_raw,
-                                      reqs[i].cfg_kwargs["codec"])
-            assert n > 0
+            data = r.data.numpy() if hasattr(r.data, "numpy") else r.data
+            shards_raw, _ = run_oracle(cfg, data, quirks=False)
+            checked, _, _ = compare_decoded(r.config(), mixed[i], shards_raw,
+                                            r.cfg_kwargs["codec"])
+            assert checked > 0
     finally:
         for s in alone_sinks + mix_sinks:
+            s.close()
+
+
+def test_admission_respects_the_budget():
+    """Three requests of one configuration and a budget for one stream of it
+    (each stream with its own encoders, charged its full estimate): they
+    are served one at a time, and the second and third reuse the first's
+    stream."""
+    from chucky_gb300 import serve
+    sinks = [MemSink() for _ in range(3)]
+    try:
+        first = _requests(sinks[:1])[0]
+        reqs = [serve.Request(name=f"{i}:{first.name}", cfg_kwargs=first.cfg_kwargs,
+                              dims=first.dims, data=first.data,
+                              frame_bytes=first.frame_bytes, sink=s.base)
+                for i, s in enumerate(sinks)]
+        budget = serve.memory_estimate(reqs[0])
+        st = serve.run_served(reqs, hbm_budget=budget, max_streams=16, paced=False,
+                              batch_encoders=False, warmup=False)
+        assert st["streams_created"] == 1 and st["streams_reused"] == 2
+        assert st["requests"] == 3
+        assert st["peak_open"] == 1
+        assert st["peak_resident_bytes"] <= budget
+    finally:
+        for s in sinks:
             s.close()

@@ -230,10 +230,30 @@ def test_gpu_store_reads_back(tmp_path, name, codec, level):
     for k in t_ora:
         if codec == "none" or k.endswith("zarr.json"):
             assert t_gpu[k] == t_ora[k], f"{k} differs"
-    nlod = H.plan_info(cfg).nlod if multiscale else 1
-    for lv in range(nlod):
-        p_gpu = os.path.join(d_gpu, str(lv))
-        p_ora = os.path.join(d_ora, str(lv))
-        np.testing.assert_array_equal(Z.read_array(p_gpu), Z.read_array(p_ora))
+    # every chunk of every shard file decodes to the oracle's chunk bytes;
+    # the slot count per shard comes from the planner: at levels >= 1 of a
+    # bounded, downsampled append dim the reference's zarr.json declares
+    # more inner chunks per shard than its epoch-split shard files hold
+    # (reproduced byte for byte), so zarr.json is not used for them
+    info = H.plan_info(cfg)
+    for k in t_ora:
+        if k.endswith("zarr.json"):
+            continue
+        lv = int(k.split(os.sep)[0]) if multiscale else 0
+        n_slots = info.chunks_per_shard_total[lv]
+        idx_g, ok_g = H.parse_shard(t_gpu[k], n_slots)
+        idx_o, ok_o = H.parse_shard(t_ora[k], n_slots)
+        assert ok_g and ok_o, k
+        for (og, ng), (oo, no) in zip(idx_g.tolist(), idx_o.tolist()):
+            assert (og == 0xFFFFFFFFFFFFFFFF) == (oo == 0xFFFFFFFFFFFFFFFF), k
+            if oo == 0xFFFFFFFFFFFFFFFF:
+                continue
+            raw = t_ora[k][oo:oo + no]
+            if codec != "none":
+                raw = H.decode(codec, raw, info.chunk_elements * 2)
+            got = t_gpu[k][og:og + ng]
+            if codec != "none":
+                got = H.decode(codec, got, info.chunk_elements * 2)
+            assert got == raw, k
     if _dense(name):
         np.testing.assert_array_equal(Z.read_array(_level0(d_gpu, multiscale)), arr)
