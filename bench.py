@@ -531,35 +531,18 @@ def _server_pass(srv, reqs, sink, paced=False):
     return e0.elapsed_time(e1)
 
 
-def served_form(reqs, lib, sink, max_streams, batch_encoders, steps, warmup,
-                budget=48 << 30):
-    """(ms per pass of the timed passes, discarded-sink bytes per pass,
-    launches, stats) of one form of the request loop."""
-    from chucky_gb300 import serve
-    with serve.Server(budget, max_streams, batch_encoders) as srv:
-        srv.prewarm(reqs, sink, per_request=max_streams > 1)
-        for _ in range(warmup):
-            srv.replay(reqs, sink, paced=False)
-        srv.reset_stats()
-        b0 = lib.chucky_discard_sink_bytes(sink)
-        l0 = lib.chucky_launch_count()
-        ms = [_server_pass(srv, reqs, sink) for _ in range(steps)]
-        launches = lib.chucky_launch_count() - l0
-        out_bytes = (lib.chucky_discard_sink_bytes(sink) - b0) / steps
-        st = srv.stats()
-    return ms, out_bytes, launches, st
-
-
-def served_latency(reqs, sink):
-    """One pass with Poisson arrivals and appends: latency and GB/s."""
-    from chucky_gb300 import serve
-    with serve.Server(48 << 30, 16, True) as srv:
-        srv.prewarm(reqs, sink, per_request=True)
+def timed_passes(srv, reqs, lib, sink, steps, warmup):
+    """(ms per timed pass, discarded-sink bytes per pass, launches) of
+    `steps` passes after `warmup` untimed ones."""
+    for _ in range(warmup):
         srv.replay(reqs, sink, paced=False)
-        srv.reset_stats()
-        ms = _server_pass(srv, reqs, sink, paced=True)
-        st = srv.stats()
-    return ms, st
+    srv.reset_stats()
+    b0 = lib.chucky_discard_sink_bytes(sink)
+    l0 = lib.chucky_launch_count()
+    ms = [_server_pass(srv, reqs, sink) for _ in range(steps)]
+    launches = lib.chucky_launch_count() - l0
+    out_bytes = (lib.chucky_discard_sink_bytes(sink) - b0) / steps
+    return ms, out_bytes, launches
 
 
 def orca_e2e(lib, dev, steps):
@@ -612,7 +595,7 @@ def orca_e2e(lib, dev, steps):
     return out
 
 
-def encoder_roofline(lib, dev, codec="lz4", reps=5):
+def encoder_roofline(lib, dev, codec="lz4", reps=5, n=64):
     """The encoder launch set alone on one 256 MiB batch of sensor chunks
     (64 chunks of 32 x 256 x 256 u16), CUDA events on its stream: bytes
     read + written per launch set and the chunk-input rate."""
@@ -630,7 +613,6 @@ def encoder_roofline(lib, dev, codec="lz4", reps=5):
     # chunk tiles 32 x 256 x 256 of the first 64 frames, as the stream lays them out
     t = frames.reshape(2, 32, 9, 256, 16, 256).permute(0, 2, 4, 1, 3, 5).contiguous()
     chunk_bytes = 32 * 256 * 256 * 2
-    n = 64
     chunks = t.reshape(-1).view(torch.uint8)[: n * chunk_bytes]
     pad = torch.zeros(n * chunk_bytes + 256, dtype=torch.uint8, device=dev)
     pad[: n * chunk_bytes].copy_(chunks)
@@ -693,17 +675,27 @@ def run_served_bench(args, rank, world):
     nbytes = sum(r.buffer()[1] for r in host_reqs)
 
     clocks = Clocks()
-    if rank == 0:
-        clocks.start()
-    ms_dev, out_b, launches, st_dev = served_form(dev_reqs, lib, sink, 16, True,
-                                                   args.steps, args.warmup)
-    ms_host, out_h, _, st_host = served_form(host_reqs, lib, sink, 16, True,
-                                             args.steps, max(1, args.warmup // 2))
-    clk = clocks.stop() if rank == 0 else None
-    pms_dev, _, _, _ = served_form(dev_reqs, lib, sink, 1, False, args.steps, args.warmup)
-    pms_host, _, _, _ = served_form(host_reqs, lib, sink, 1, False, args.steps,
-                                    max(1, args.warmup // 2))
-    lat_ms, lat = served_latency(host_reqs, sink)
+    # the served form: one server (start-up: a resident stream per request),
+    # device-input passes, host-input passes, then the paced latency pass
+    with serve.Server(48 << 30, 16, True) as srv:
+        srv.prewarm(host_reqs, sink, per_request=True)
+        if rank == 0:
+            clocks.start()
+        ms_dev, out_b, launches = timed_passes(srv, dev_reqs, lib, sink, args.steps,
+                                               args.warmup)
+        st_dev = srv.stats()
+        ms_host, out_h, _ = timed_passes(srv, host_reqs, lib, sink, args.steps,
+                                         max(1, args.warmup // 2))
+        clk = clocks.stop() if rank == 0 else None
+        srv.reset_stats()
+        lat_ms = _server_pass(srv, host_reqs, sink, paced=True)
+        lat = srv.stats()
+    # the plain form: one request at a time, each stream encoding on its own
+    with serve.Server(1 << 62, 1, False) as psrv:
+        psrv.prewarm(host_reqs, sink, per_request=False)
+        pms_dev, _, _ = timed_passes(psrv, dev_reqs, lib, sink, args.steps, args.warmup)
+        pms_host, _, _ = timed_passes(psrv, host_reqs, lib, sink, args.steps,
+                                      max(1, args.warmup // 2))
     link = h2d_probe([r.data for r in host_reqs[:4]], [r.data for r in dev_reqs[:4]], dev)
     lib.chucky_discard_sink_destroy(sink)
     del dev_reqs
@@ -953,6 +945,13 @@ def run_single(args):
     lib.chucky_discard_sink_create.restype = C.c_void_p
     lib.chucky_discard_sink_destroy.argtypes = [C.c_void_p]
     lib.tile_stream_gpu_restart.argtypes = [C.c_void_p, C.c_void_p]
+    if args.single in ("encode-lz4", "encode-zstd"):
+        # the encoder launch set alone on a batch of sensor chunks (48 chunks
+        # of 32 x 256 x 256 u16, 192 MiB: more than L2): the ncu case
+        enc = encoder_roofline(lib, torch.device("cuda"), args.single.split("-")[1],
+                               reps=args.steps, n=48)
+        print("ok", round(enc["input_gbs"], 1), flush=True)
+        return
     if args.single in ("u16", "f32"):
         u16, f32 = make_cubes()
         cube = u16 if args.single == "u16" else f32
@@ -995,7 +994,7 @@ def main():
     ap.add_argument("--frames", type=int, default=512,
                     help="sensor frames per step (multiple of 32)")
     ap.add_argument("--single", choices=["u16", "f32", "cube-lz4", "sensor-zstd",
-                                         "sensor-lz4"],
+                                         "sensor-lz4", "encode-lz4", "encode-zstd"],
                     help="profiling case: one array's stream, --steps passes, no timing")
     args = ap.parse_args()
     if args.single:

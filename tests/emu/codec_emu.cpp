@@ -227,6 +227,54 @@ int main(int argc, char** argv)
       }
     }
   }
+  if (argc > 6 && std::string(argv[6]) == "refs") {
+    // The same chunks addressed one by one (CodecBatch::refs, as the shared
+    // encoder engine gathers several streams' chunks): chunks in reverse
+    // order in a buffer of another stride, outputs and sizes in reverse
+    // slots of other buffers.  Every chunk must decode to its bytes.  (The
+    // bytes themselves may differ from the first run here: the emulation
+    // resolves stores of several lanes to one hash slot in thread order,
+    // which varies from run to run; the GPU keeps one lane's store.)
+    const uint64_t st2 = in_stride + 64, os2 = out_stride + 32;
+    std::vector<uint8_t> in2(n * st2 + 256), out2(n * os2 + 64);
+    std::vector<uint64_t> sizes2(n, 0);
+    std::vector<ChunkRef> refs(n);
+    for (uint64_t c = 0; c < n; ++c) {
+      const uint64_t r = n - 1 - c;
+      std::memcpy(in2.data() + r * st2, flat.data() + c * chunk, chunk);
+      refs[c].in = in2.data() + r * st2;
+      refs[c].out = out2.data() + r * os2;
+      refs[c].size = sizes2.data() + r;
+    }
+    CodecBatch rb{};
+    rb.chunk_bytes = chunk;
+    rb.n_chunks = n;
+    rb.level = 1;
+    rb.refs = refs.data();
+    std::vector<uint8_t> scratch2(sb, 0x5A);
+    if ((codec == "zstd" ? launch_zstd(rb, scratch2.data(), nullptr)
+                         : launch_lz4(rb, scratch2.data(), nullptr)) != cudaSuccess)
+      return 1;
+    for (uint64_t c = 0; c < n; ++c) {
+      const uint64_t r = n - 1 - c;
+      const uint8_t* src = out2.data() + r * os2;
+      size_t got = 0;
+      if (codec == "zstd") {
+        got = zd(dec.data(), dec.size(), src, sizes2[r]);
+        if (ze(got))
+          got = 0;
+      } else {
+        const int k = ld((const char*)src, (char*)dec.data(), int(sizes2[r]), int(chunk));
+        got = k < 0 ? 0 : size_t(k);
+      }
+      if (sizes2[r] == 0 || sizes2[r] > bound || got != chunk ||
+          std::memcmp(dec.data(), flat.data() + c * chunk, chunk)) {
+        std::fprintf(stderr, "chunk %llu: refs addressing: size %llu, decoded %zu bytes\n",
+                     (unsigned long long)c, (unsigned long long)sizes2[r], got);
+        return 1;
+      }
+    }
+  }
   std::printf("ok %s chunk=%u n=%llu pattern=%s ratio=%.3f\n", codec.c_str(), chunk,
               (unsigned long long)n, pat.c_str(), double(n * chunk) / double(comp));
   return 0;

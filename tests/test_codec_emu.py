@@ -46,8 +46,8 @@ BIG = [("zstd", "xor16", 200000, 1), ("zstd", "mixed", 131072, 2),
        ("lz4", "halves", 300000, 2), ("lz4", "random", 270000, 1)]
 
 
-def _run(emu, codec, pattern, chunk, n):
-    r = subprocess.run([emu, codec, str(chunk), str(n), pattern, "7"],
+def _run(emu, codec, pattern, chunk, n, *extra):
+    r = subprocess.run([emu, codec, str(chunk), str(n), pattern, "7", *extra],
                        capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stderr[-2000:]
     assert r.stdout.startswith("ok")
@@ -63,3 +63,13 @@ def test_encoder_multi_block_chunks(emu, codec, pattern, chunk, n):
 @pytest.mark.parametrize("chunk,n", CASES)
 def test_encoder_decodes_with_stock_library(emu, codec, pattern, chunk, n):
     _run(emu, codec, pattern, chunk, n)
+
+
+@pytest.mark.parametrize("codec,pattern,chunk,n", [("zstd", "mixed", 70000, 3),
+                                                  ("lz4", "mixed", 70000, 3),
+                                                  ("zstd", "xor16", 1024, 5),
+                                                  ("lz4", "random", 37, 4)])
+def test_encoder_per_chunk_references(emu, codec, pattern, chunk, n):
+    """Chunks addressed through a per-chunk reference list (the shared
+    encoder engine's batches) decode to their bytes."""
+    _run(emu, codec, pattern, chunk, n, "refs")
