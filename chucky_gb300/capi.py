@@ -205,7 +205,8 @@ def bind_zarr_fs_sink(lib):
 # include/chucky_serve.h (served form; no reference counterpart)
 class ServerConfig(C.Structure):
     _fields_ = [("hbm_budget_bytes", C.c_size_t), ("max_streams", C.c_int),
-                ("batch_encoders", C.c_int), ("encoder_wave_bytes", C.c_size_t)]
+                ("batch_encoders", C.c_int), ("encoder_wave_bytes", C.c_size_t),
+                ("encoder_lanes", C.c_int)]
 
 
 class ServerStats(C.Structure):

@@ -29,12 +29,13 @@ static_assert(sizeof(ChunkRef) % 4 == 0, "references travel as 32-bit words");
 
 } // namespace
 
-int Engine::init(uint64_t wave_bytes)
+int Engine::init(uint64_t wave_bytes, int lanes)
 {
   ECK(cudaGetDevice(&device_));
   wave_bytes_ = wave_bytes;
-  for (Lane& L : lane_)
-    ECK(cudaStreamCreateWithFlags(&L.st, cudaStreamNonBlocking));
+  lanes_ = std::max(1, std::min(lanes, kMaxLanes));
+  for (int i = 0; i < lanes_; ++i)
+    ECK(cudaStreamCreateWithFlags(&lane_[i].st, cudaStreamNonBlocking));
   h_refs_cap_ = 1 << 14;
   for (int i = 0; i < kHostRefSlots; ++i) {
     ECK(cudaHostAlloc(&h_refs_[i], h_refs_cap_ * sizeof(ChunkRef), cudaHostAllocMapped));
@@ -130,7 +131,7 @@ int Engine::reserve_scratch(Lane& L, size_t bytes)
 int Engine::process(std::vector<EncodeJob*>& jobs)
 {
   Lane& L = lane_[next_lane_];
-  next_lane_ = (next_lane_ + 1) % kLanes;
+  next_lane_ = (next_lane_ + 1) % lanes_;
   for (EncodeJob* j : jobs) {
     ECK(cudaStreamWaitEvent(L.st, j->ready, 0));
     if (j->out_free)

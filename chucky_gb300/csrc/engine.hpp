@@ -62,8 +62,10 @@ class Engine
 {
 public:
   // Scratch and reference lists for waves of up to wave_bytes of input, on
-  // the current device.  Returns 0 on success.
-  int init(uint64_t wave_bytes);
+  // the current device, with `lanes` engine CUDA streams (1..kMaxLanes;
+  // consecutive rounds go to consecutive lanes and may overlap on the
+  // device).  Returns 0 on success.
+  int init(uint64_t wave_bytes, int lanes);
   ~Engine();
 
   // Enqueue the job's encoders with the next round; returns once they are
@@ -81,7 +83,7 @@ private:
     ChunkRef* d_refs = nullptr;
     uint64_t refs_cap = 0;
   };
-  static constexpr int kLanes = 2;
+  static constexpr int kMaxLanes = 8;
   static constexpr int kHostRefSlots = 8;
 
   void loop();
@@ -91,7 +93,8 @@ private:
 
   int device_ = 0;
   uint64_t wave_bytes_ = 0;
-  Lane lane_[kLanes];
+  Lane lane_[kMaxLanes];
+  int lanes_ = 2;
   int next_lane_ = 0;
   // pinned host staging of reference lists, each reused after its copy to
   // the device has run

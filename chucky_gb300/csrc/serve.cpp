@@ -121,7 +121,8 @@ chucky_server_create(const chucky_server_config* config)
     s->engine.reset(new (std::nothrow) chucky::Engine());
     const uint64_t wave = config->encoder_wave_bytes ? config->encoder_wave_bytes
                                                      : (256ull << 20);
-    if (!s->engine || s->engine->init(wave)) {
+    const int lanes = config->encoder_lanes > 0 ? config->encoder_lanes : 2;
+    if (!s->engine || s->engine->init(wave, lanes)) {
       delete s;
       return nullptr;
     }

@@ -146,7 +146,9 @@ int Stream::init(const tile_stream_configuration* c, shard_sink* sk)
     CK(cudaEventRecord(ev_input_free[i], s_comp));
   }
   stage_bytes = staging_slot_bytes(cfg.buffer_capacity_bytes);
-  stage_small = stage_bytes;
+  // a CPU copy into the ring costs about what a direct copy's wait does at
+  // a few hundred KiB: larger pinned appends are copied directly
+  stage_small = std::min<uint64_t>(stage_bytes, 256u << 10);
   for (int i = 0; i < kStageSlots; ++i) {
     CK(cudaHostAlloc(&h_stage[i], stage_bytes, cudaHostAllocDefault));
     CK(cudaEventCreateWithFlags(&ev_stage[i], cudaEventDisableTiming));
@@ -743,7 +745,11 @@ int Stream::kick_batch(uint32_t n_epochs, const uint32_t* epoch_masks)
     // be done before the encoders overwrite it
     CK(cudaStreamWaitEvent(se, ev_agg_done[si], 0));
     if (engine) {
-      // the shared engine encodes this batch with other streams' batches
+      // the shared engine encodes this batch with other streams' batches.
+      // The job goes to the engine once its chunks are in the pool, so the
+      // engine's launches never wait on the device for one stream's epoch
+      // kernels while other streams' chunks are ready.
+      CK(cudaEventSynchronize(ev_pool_ready));
       EncodeJob& J = job[si];
       J = EncodeJob{};
       J.codec = cfg.codec.id;

@@ -78,7 +78,8 @@ struct Stream
   int stage_cur = 0;         // slot being filled
   uint64_t stage_fill = 0;   // bytes in it not yet issued
   uint8_t* stage_dst = nullptr; // device destination of its first byte
-  // appends of pinned host memory up to this size go through the ring
+  // appends of pinned host memory up to this size (256 KiB at most) go
+  // through the ring
   uint64_t stage_small = 0;
   // stream-ordered appends of device memory (append_async)
   cudaEvent_t ev_producer = nullptr, ev_consumed = nullptr;

@@ -45,6 +45,7 @@ extern "C"
     int max_streams;         /* requests open at once (>= 1) */
     int batch_encoders;      /* 1: shared encoder engine across streams */
     size_t encoder_wave_bytes; /* engine launch size (0: 256 MiB of input) */
+    int encoder_lanes;         /* engine CUDA streams, rounds overlap (0: 2) */
   };
 
   struct chucky_server;
