@@ -547,7 +547,10 @@ def timed_passes(srv, reqs, lib, sink, steps, warmup):
 
 def orca_e2e(lib, dev, steps):
     """The Orca-shaped sensor stream (zstd-1, 5-level dim-0 max pyramid),
-    512 frames appended frame by frame from pinned host memory."""
+    512 frames from pinned host memory, appended in pieces of 32 Mi
+    elements as the reference's benchmark pumps its input
+    (bench/bench_util.c:673, tests/test_data.c:138-160), and frame by
+    frame."""
     import torch
     import chucky_gb300 as cg
     frames = sensor_frames(ORCA_FRAMES, dev)
@@ -558,7 +561,7 @@ def orca_e2e(lib, dev, steps):
     s = cg.GpuStream(sensor_config("zstd", "max"), sink)
     frame = SENSOR_H * SENSOR_W * 2
 
-    def one():
+    def one(piece):
         if lib.tile_stream_gpu_restart(s.h, None) != 0:
             raise RuntimeError("restart failed")
         e0 = torch.cuda.Event(enable_timing=True)
@@ -566,8 +569,8 @@ def orca_e2e(lib, dev, steps):
         torch.cuda.synchronize()
         e0.record()
         base = host.data_ptr()
-        for a in range(0, host.numel(), frame):
-            if s.append(base + a, frame).error:
+        for a in range(0, host.numel(), piece):
+            if s.append(base + a, min(piece, host.numel() - a)).error:
                 raise RuntimeError("append failed")
         if s.flush().error:
             raise RuntimeError("flush failed")
@@ -575,23 +578,76 @@ def orca_e2e(lib, dev, steps):
         torch.cuda.synchronize()
         return e0.elapsed_time(e1)
 
+    pump = 32 << 21  # 32 Mi u16 elements
     for _ in range(2):
-        one()
-    ms = [one() for _ in range(steps)]
+        one(pump)
+    ms = [one(pump) for _ in range(steps)]
+    ms_frames = [one(frame) for _ in range(max(2, steps // 2))]
     link = h2d_probe([host], [dbuf], dev)
     s.close()
     lib.chucky_discard_sink_destroy(sink)
     gbs = host.numel() * len(ms) / (sum(ms) * 1e-3) / 1e9
+    gbs_frames = host.numel() * len(ms_frames) / (sum(ms_frames) * 1e-3) / 1e9
     out = {"workload": "%d u16 frames 2304x4096 (seeded Poisson(100) + 64 Gaussian blobs), "
                        "chunk 32x256x256, shard 32x2048x2048, 5-level (t,y,x) max pyramid "
-                       "with dim-0 downsampling, zstd-1, K=%d, appended frame by frame from "
-                       "pinned host memory" % (ORCA_FRAMES, EPOCHS_PER_BATCH),
+                       "with dim-0 downsampling, zstd-1, K=%d, pinned host memory appended "
+                       "in 64 MiB pieces (32 Mi elements, the reference benchmark's pump)"
+                       % (ORCA_FRAMES, EPOCHS_PER_BATCH),
            "value": round(gbs, 3), "unit": "GB/s", "steps": len(ms),
+           "frame_by_frame": round(gbs_frames, 3),
            "ms_per_step": round(float(np.mean(ms)), 3),
            "h2d_link_gbs": round(link, 2), "link_note": SERVED_LINK_NOTE,
            "frac_of_h2d_link": round(gbs / link, 4) if link else None}
     del frames, dbuf, host
     torch.cuda.empty_cache()
+    return out
+
+
+def cube_appends(lib, dev, steps):
+    """The 256^3 u16 LZ4 cube (chunk 64^3, one shard, no pyramid) through
+    writer_append from host memory in three ways: 256 appends of one
+    256 x 256 frame from pinned memory and from pageable memory (both go
+    through the stream's pinned staging ring), and the whole cube in one
+    append from pageable memory (as the reference's benchmark pumps a
+    malloc'd buffer).  GB/s of input, each way timed on the device around
+    whole passes."""
+    import torch
+    import chucky_gb300 as cg
+    u16, _ = make_cubes()
+    pageable = np.ascontiguousarray(u16).view(np.uint8).reshape(-1)
+    pinned = torch.from_numpy(pageable.copy()).pin_memory()
+    sink = lib.chucky_discard_sink_create()
+    s = cg.GpuStream(cube_lz4_config(), sink)
+    frame = SIDE * SIDE * 2
+    out = {}
+    for name, base, step in (("frames_pinned", pinned.data_ptr(), frame),
+                             ("frames_pageable", pageable.ctypes.data, frame),
+                             ("whole_pageable", pageable.ctypes.data, pageable.size)):
+        def one():
+            if lib.tile_stream_gpu_restart(s.h, None) != 0:
+                raise RuntimeError("restart failed")
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record()
+            for a in range(0, pageable.size, step):
+                if s.append(base + a, min(step, pageable.size - a)).error:
+                    raise RuntimeError("append failed")
+            if s.flush().error:
+                raise RuntimeError("flush failed")
+            e1.record()
+            torch.cuda.synchronize()
+            return e0.elapsed_time(e1)
+        for _ in range(2):
+            one()
+        ms = [one() for _ in range(steps)]
+        out[name] = round(pageable.size * len(ms) / (sum(ms) * 1e-3) / 1e9, 3)
+    s.close()
+    lib.chucky_discard_sink_destroy(sink)
+    out["workload"] = ("256^3 u16 (xor + noise), chunk 64^3, one shard of 4^3 chunks, no "
+                       "pyramid, LZ4, K=%d; frames = 256 appends of 256 x 256" %
+                       CUBE_EPOCHS_PER_BATCH)
+    out["unit"] = "GB/s"
     return out
 
 
@@ -648,9 +704,9 @@ def encoder_roofline(lib, dev, codec="lz4", reps=5, n=64):
 
 
 # DRAM bytes (read + written) per byte of chunk input of the LZ4 launch set
-# on sensor chunks, from the ncu capture summarised in
-# profiles/lz4_encoder_sensor_chunks.md (scaled to the launch's input)
-LZ4_SENSOR_TRAFFIC_PER_INPUT_BYTE = None
+# (find + emit) on sensor chunks, from one ncu capture of 48 chunks of
+# 32 x 256 x 256 u16 (`--single encode-lz4`)
+LZ4_SENSOR_TRAFFIC_PER_INPUT_BYTE = (209.0 + 268.5 + 527.8 + 144.2) / 201.3
 
 
 def run_served_bench(args, rank, world):
@@ -701,6 +757,7 @@ def run_served_bench(args, rank, world):
     del dev_reqs
     torch.cuda.empty_cache()
     orca = orca_e2e(lib, dev, max(3, args.steps // 2))
+    cube = cube_appends(lib, dev, max(3, args.steps // 2))
     enc = encoder_roofline(lib, dev, "lz4")
     enc_z = encoder_roofline(lib, dev, "zstd")
 
@@ -751,6 +808,7 @@ def run_served_bench(args, rank, world):
             "engine_max_jobs_per_round")},
         "compression_ratio": round(nbytes / max(1.0, out_b), 4),
         "orca_e2e": orca,
+        "cube_appends": cube,
         "roofline": {"kernel": "lz4 encoder launch set (find+plan+emit) on 64 sensor "
                                "chunks of 32x256x256 u16, timed alone",
                      "bound": "hbm", "limiter": "compute (match finding and sequence "
@@ -758,7 +816,9 @@ def run_served_bench(args, rank, world):
                      "achieved": round(enc["achieved_gbs"], 2), "peak": peak,
                      "unit": "GB/s", "frac": round(enc["achieved_gbs"] / peak, 4),
                      "peak_source": peak_src, "traffic": traffic,
-                     "traffic_note": ("ncu DRAM bytes of the same launch set, per launch"
+                     "traffic_note": ("ncu DRAM bytes read + written by lz4_find_k + "
+                                      "lz4_emit_k per input byte, one capture on 48 "
+                                      "sensor chunks, scaled to this launch set's input"
                                       if traffic else "not captured"),
                      "input_gbs": round(enc["input_gbs"], 2),
                      "ms_per_launch_set": round(enc["ms"], 4)},
@@ -801,7 +861,11 @@ def cpu_request_step(req, threads):
 
 
 def served_sample():
-    """One request of each of the four shapes (as drawn for the workload)."""
+    """One request of each of the four shapes (as drawn for the workload),
+    with the reference's default epochs per batch (chosen from its target of
+    1024 chunks per batch, src/stream/config.c:31-45) rather than the GPU
+    streams' two or four."""
+    import dataclasses
     from chucky_gb300 import serve
     reqs = serve.c5_requests(pinned=False)
     out, seen = [], set()
@@ -809,7 +873,8 @@ def served_sample():
         kind = r.name.split(":")[1]
         if kind not in seen:
             seen.add(kind)
-            out.append(r)
+            kw = dict(r.cfg_kwargs, epochs_per_batch=0)
+            out.append(dataclasses.replace(r, cfg_kwargs=kw, _cfg=None))
     return out
 
 
@@ -828,7 +893,8 @@ def cpu_baseline_served(args):
             "sample": f"{passes} pass(es) over one request of each of the four shapes "
                       f"({', '.join(r.name for r in sample)}; {tot_b / passes / 1e9:.2f} GB "
                       f"per pass, {tot_t:.1f} s) through the oracle/ restatement of the "
-                      "reference CPU backend (LZ4-HC / zstd from the system libraries)"}
+                      "reference CPU backend (LZ4-HC / zstd from the system libraries), "
+                      "epochs per batch at the reference's default"}
 
 
 def run_reference_served(args, rank, world):
@@ -854,7 +920,8 @@ def run_reference_served(args, rank, world):
             "dtype": "u8+u16+f32", "data": "synthetic",
             "config": {"workload": desc, "same_config": True,
                        "sample": "each step: one request of each of the four shapes "
-                                 "(bounded CPU sample of the same workload)"},
+                                 "(bounded CPU sample of the same workload), epochs per "
+                                 "batch at the reference's default"},
             "cpu_baseline": {"value": round(v, 4), "unit": "GB/s", "cores": threads,
                              "kind": "port",
                              "sample": "one request per shape per step through the "
@@ -945,6 +1012,28 @@ def run_single(args):
     lib.chucky_discard_sink_create.restype = C.c_void_p
     lib.chucky_discard_sink_destroy.argtypes = [C.c_void_p]
     lib.tile_stream_gpu_restart.argtypes = [C.c_void_p, C.c_void_p]
+    if args.single == "served-pass":
+        # one pass of the served workload (device inputs) after the server's
+        # start-up and one warm-up pass: the launch-list case
+        import dataclasses
+        from chucky_gb300 import serve
+        slib = serve._lib()
+        dev = torch.device("cuda")
+        host = serve.c5_requests()
+        on_dev = {}
+        for r in host:
+            if id(r.data) not in on_dev:
+                on_dev[id(r.data)] = r.data.to(dev)
+        reqs = [dataclasses.replace(r, data=on_dev[id(r.data)], _cfg=None) for r in host]
+        sink = slib.chucky_discard_sink_create()
+        with serve.Server(48 << 30, 16, True) as srv:
+            srv.prewarm(reqs, sink, per_request=True)
+            for _ in range(1 + args.steps):
+                srv.replay(reqs, sink, paced=False)
+            torch.cuda.synchronize()
+        slib.chucky_discard_sink_destroy(sink)
+        print("ok", flush=True)
+        return
     if args.single in ("encode-lz4", "encode-zstd"):
         # the encoder launch set alone on a batch of sensor chunks (48 chunks
         # of 32 x 256 x 256 u16, 192 MiB: more than L2): the ncu case
@@ -994,7 +1083,8 @@ def main():
     ap.add_argument("--frames", type=int, default=512,
                     help="sensor frames per step (multiple of 32)")
     ap.add_argument("--single", choices=["u16", "f32", "cube-lz4", "sensor-zstd",
-                                         "sensor-lz4", "encode-lz4", "encode-zstd"],
+                                         "sensor-lz4", "encode-lz4", "encode-zstd",
+                                         "served-pass"],
                     help="profiling case: one array's stream, --steps passes, no timing")
     args = ap.parse_args()
     if args.single:

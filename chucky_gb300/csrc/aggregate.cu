@@ -164,6 +164,161 @@ __global__ void __launch_bounds__(256) tail_copy_k(TailCopies t)
   }
 }
 
+// ---- shard index and crc32c ------------------------------------------------
+
+constexpr uint32_t kCrcPoly = 0x82F63B78u; // Castagnoli, reflected
+constexpr int kIndexThreads = 128;
+
+// a * b mod P in the reflected representation (bit 31 = x^0); `a` is a
+// power of x (never 0).  The combination of segment CRCs through
+// multiplication by x^(8 n) mod P is the published method of zlib's
+// crc32_combine (M. Adler).
+__device__ uint32_t crc_mulmod(uint32_t a, uint32_t b)
+{
+  uint32_t p = 0;
+  for (int i = 0; i < 32; ++i) {
+    if (a & (0x80000000u >> i))
+      p ^= b;
+    b = (b & 1) ? (b >> 1) ^ kCrcPoly : b >> 1;
+  }
+  return p;
+}
+
+// x^(8 n) mod P
+__device__ uint32_t crc_xpow8(uint64_t n)
+{
+  uint32_t p = 0x80000000u, base = 0x00800000u; // x^0, x^8
+  while (n) {
+    if (n & 1)
+      p = crc_mulmod(p, base);
+    base = crc_mulmod(base, base);
+    n >>= 1;
+  }
+  return p;
+}
+
+// crc32c of the index words idx[0 .. nwords) (u64, little endian), by the
+// whole CTA: one segment per thread, combined by thread 0.
+__device__ uint32_t index_crc32c(const uint64_t* idx, uint64_t nwords, uint32_t* table,
+                                 uint32_t* part)
+{
+  const unsigned tid = threadIdx.x, nt = blockDim.x;
+  const uint64_t per = (nwords + nt - 1) / nt; // words per thread
+  const uint64_t w0 = (tid * per < nwords ? tid * per : nwords), w1 = (w0 + per < nwords ? w0 + per : nwords);
+  uint32_t c = 0;
+  for (uint64_t w = w0; w < w1; ++w) {
+    uint64_t v = idx[w];
+    for (int k = 0; k < 8; ++k) {
+      c = table[(c ^ uint32_t(v)) & 0xFF] ^ (c >> 8);
+      v >>= 8;
+    }
+  }
+  part[tid] = c;
+  __syncthreads();
+  uint32_t crc = 0;
+  if (tid == 0) {
+    uint32_t st = 0xFFFFFFFFu;
+    const uint32_t xfull = crc_xpow8(per * 8);
+    for (unsigned t = 0; t < nt; ++t) {
+      const uint64_t a = t * per < nwords ? t * per : nwords;
+      const uint64_t b = a + per < nwords ? a + per : nwords;
+      if (b <= a)
+        break;
+      const uint32_t x = (b - a == per) ? xfull : crc_xpow8((b - a) * 8);
+      st = crc_mulmod(x, st) ^ part[t];
+    }
+    crc = st ^ 0xFFFFFFFFu;
+  }
+  __syncthreads();
+  return crc;
+}
+
+// A CTA per (level, shard) (shards beyond the grid's y extent looped): the
+// level's runs in order (each shard's cursor depends on the runs before),
+// the entries of a run in parallel.
+__global__ void __launch_bounds__(kIndexThreads) index_k(IndexBatch b)
+{
+  __shared__ uint32_t table[256];
+  __shared__ uint32_t part[kIndexThreads];
+  __shared__ uint32_t crc_sh;
+  const IndexLevel& L = b.lv[blockIdx.x];
+  const unsigned tid = threadIdx.x, nt = blockDim.x;
+  if (blockIdx.y >= L.shards)
+    return;
+  for (unsigned i = tid; i < 256; i += nt) {
+    uint32_t c = i;
+    for (int k = 0; k < 8; ++k)
+      c = (c & 1) ? (c >> 1) ^ kCrcPoly : c >> 1;
+    table[i] = c;
+  }
+  __syncthreads();
+  const uint64_t sa = b.alignment;
+  const uint64_t nidx = L.cps_total * 16, total = nidx + 4;
+  const uint64_t pad = L.blob_bytes - total;
+  const uint64_t cpi = L.cpi;
+  for (uint64_t s = blockIdx.y; s < L.shards; s += gridDim.y) {
+    uint64_t* idx = L.index + s * L.cps_total * 2;
+    uint64_t cur = L.cursor[s];
+    uint32_t nfinal = 0;
+    // the shard's final index blob: padding, index, crc32c; then reset
+    auto finalize = [&](uint8_t* blob) {
+      const uint32_t crc = index_crc32c(idx, L.cps_total * 2, table, part);
+      if (tid == 0)
+        crc_sh = crc;
+      __syncthreads();
+      for (uint64_t i = tid; i < pad; i += nt)
+        blob[i] = 0;
+      if ((pad & 3) == 0) {
+        uint32_t* d = reinterpret_cast<uint32_t*>(blob + pad);
+        const uint32_t* w = reinterpret_cast<const uint32_t*>(idx);
+        for (uint64_t i = tid; i < nidx / 4; i += nt)
+          d[i] = w[i];
+      } else {
+        const uint8_t* src = reinterpret_cast<const uint8_t*>(idx);
+        for (uint64_t i = tid; i < nidx; i += nt)
+          blob[pad + i] = src[i];
+      }
+      if (tid < 4)
+        blob[pad + nidx + tid] = uint8_t(crc_sh >> (8 * tid));
+      __syncthreads();
+      for (uint64_t i = tid; i < L.cps_total * 2; i += nt)
+        idx[i] = ~uint64_t(0);
+      __syncthreads();
+    };
+    if (L.flush) {
+      finalize(L.blobs + s * L.blob_bytes);
+      cur = 0;
+    } else {
+      for (uint32_t r = 0; r < L.n_runs; ++r) {
+        const IndexRun R = L.runs[r];
+        const uint64_t j0 = s * L.n_active * cpi + uint64_t(R.a0) * cpi;
+        const uint64_t j1 = j0 + uint64_t(R.run) * cpi;
+        const uint64_t base = L.offsets[j0];
+        const uint64_t nbytes = L.offsets[j1] - base;
+        for (uint64_t t = tid; t < uint64_t(R.run) * cpi; t += nt) {
+          const uint64_t j = j0 + t;
+          const uint64_t rs = L.real_sizes[j];
+          if (rs > 0) {
+            const uint64_t slot = (uint64_t(R.eis0) + t / cpi) * cpi + t % cpi;
+            idx[2 * slot] = cur + (L.offsets[j] - base);
+            idx[2 * slot + 1] = rs;
+          }
+        }
+        __syncthreads();
+        cur += sa ? (nbytes + sa - 1) / sa * sa : nbytes;
+        if (R.final) {
+          finalize(L.blobs + (uint64_t(nfinal) * L.shards + s) * L.blob_bytes);
+          ++nfinal;
+          cur = 0;
+        }
+      }
+    }
+    if (tid == 0)
+      L.cursor[s] = cur;
+    __syncthreads();
+  }
+}
+
 __global__ void stage_copy_k(uint32_t* dst, const uint32_t* src, uint64_t n)
 {
   for (uint64_t i = blockIdx.x * uint64_t(blockDim.x) + threadIdx.x; i < n;
@@ -217,6 +372,17 @@ cudaError_t launch_tail_copy(const TailCopies& t, uint64_t max_bytes, cudaStream
   const uint64_t cap = uint64_t(device_sm_count()) * 2;
   const dim3 grid(unsigned(pieces < cap ? pieces : cap), unsigned(t.n));
   tail_copy_k<<<grid, 256, 0, st>>>(t);
+  note_launches(1);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_index(const IndexBatch& b, cudaStream_t st)
+{
+  if (b.nlevels <= 0 || !b.max_shards)
+    return cudaSuccess;
+  const uint64_t ys = b.max_shards < 65535 ? b.max_shards : 65535;
+  const dim3 grid(unsigned(b.nlevels), unsigned(ys));
+  index_k<<<grid, kIndexThreads, 0, st>>>(b);
   note_launches(1);
   return cudaGetLastError();
 }

@@ -136,6 +136,45 @@ cudaError_t launch_aggregate(const AggBatch& b,
                              uint64_t* scratch, // >= max positions
                              cudaStream_t st);
 
+// Shard index (src/zarr/shard_delivery.c:36-102), built on the device.
+// Per level the index of every shard of the current shard epoch
+// (cps_total (offset, nbytes) u64 pairs, all ones for an empty slot) and
+// each shard's file cursor stay resident on the device.  A batch's runs of
+// consecutive active epochs add their chunks' entries; a run that completes
+// the shard epoch then writes every shard's final index blob -- zero
+// padding to the alignment, the index, its crc32c -- and resets the state.
+struct IndexRun
+{
+  uint32_t a0;    // first active epoch of the run within the batch
+  uint32_t run;   // epochs
+  uint32_t eis0;  // epoch in shard of its first epoch
+  uint32_t final; // the run completes the shard epoch
+};
+struct IndexLevel
+{
+  uint64_t* index;             // [shards][cps_total][2] (device)
+  uint64_t* cursor;            // [shards] bytes in each shard file so far
+  const uint64_t* offsets;     // the batch's shard-order offsets (or null)
+  const uint64_t* real_sizes;  // pre-padding sizes
+  const IndexRun* runs;        // [n_runs]
+  uint32_t n_runs;
+  uint32_t n_active;           // active epochs of the level in the batch
+  uint64_t cpi;                // chunks per shard per epoch (inner)
+  uint64_t cps_total;          // index entries per shard
+  uint64_t shards;             // shards per shard epoch
+  uint8_t* blobs;              // [finalisations][shards][blob_bytes] (mapped)
+  uint64_t blob_bytes;         // padded index + crc32c
+  int flush;                   // finalise every shard now (no runs)
+};
+struct IndexBatch
+{
+  uint64_t alignment;
+  int nlevels;
+  uint64_t max_shards;
+  IndexLevel lv[32];
+};
+cudaError_t launch_index(const IndexBatch& b, cudaStream_t st);
+
 // The rest of a batch's shard-ordered bytes after a copy-engine transfer of
 // the expected size: per level, bytes [start, *total) of `src` (device) to
 // `dst` (mapped host memory), where *total is the level's byte count the

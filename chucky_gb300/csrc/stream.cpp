@@ -33,8 +33,6 @@
 
 namespace chucky {
 
-uint32_t crc32c_host(const void* data, size_t len);
-
 namespace {
 
 inline uint64_t round_up(uint64_t x, uint64_t a) { return (x + a - 1) / a * a; }
@@ -463,11 +461,27 @@ int Stream::setup_aggregate()
       if (cfg.codec.id != CODEC_NONE)
         CK(cudaMalloc(&D.d_data, data));
     }
-    // shard state (src/zarr/shard_delivery.c:10-34)
+    // shard state (src/zarr/shard_delivery.c:10-34); the index lives on
+    // the device
     Shards& S = shards[l];
     S.sh.resize(V.shard_inner_count);
-    for (auto& sh : S.sh)
-      sh.index.assign(2 * V.cps_total, ~uint64_t(0));
+    const uint64_t nidx = V.cps_total * 16, itotal = nidx + 4;
+    blob_bytes[l] = sa ? round_up(itotal, sa) : itotal;
+    CK(cudaMalloc(&d_index[l], V.shard_inner_count * nidx));
+    CK(cudaMemset(d_index[l], 0xFF, V.shard_inner_count * nidx));
+    CK(cudaMalloc(&d_cursor[l], V.shard_inner_count * 8));
+    CK(cudaMemset(d_cursor[l], 0, V.shard_inner_count * 8));
+    CK(cudaHostAlloc(&h_flush_blobs[l], V.shard_inner_count * blob_bytes[l],
+                     cudaHostAllocMapped));
+    const uint32_t finals = cap_epochs / uint32_t(std::max<uint64_t>(1, V.cps_append)) + 2;
+    for (int si = 0; si < 2; ++si) {
+      DeliverySlot::Level& D = slot[si].lv[l];
+      D.runs_cap = cap_epochs + 2;
+      D.finals_cap = finals;
+      CK(cudaHostAlloc(&D.runs, D.runs_cap * sizeof(IndexRun), cudaHostAllocMapped));
+      CK(cudaHostAlloc(&D.blobs, finals * V.shard_inner_count * blob_bytes[l],
+                       cudaHostAllocMapped));
+    }
   }
   agg_scratch_slot = (max_positions + 1) * size_t(P.nlod);
   CK(cudaMalloc(&d_agg_scratch, 2 * agg_scratch_slot * 8));
@@ -507,6 +521,8 @@ void Stream::release()
     if (ev_batch[i])
       cudaEventDestroy(ev_batch[i]);
     for (int l = 0; l < LOD_MAX_LEVELS; ++l) {
+      cudaFreeHost(slot[i].lv[l].runs);
+      cudaFreeHost(slot[i].lv[l].blobs);
       cudaFreeHost(slot[i].lv[l].offsets);
       cudaFreeHost(slot[i].lv[l].real_sizes);
       cudaFreeHost(slot[i].lv[l].data);
@@ -546,6 +562,11 @@ void Stream::release()
   cudaFree(d_gather_fixed);
   cudaFree(d_agg_scratch);
   for (int l = 0; l < LOD_MAX_LEVELS; ++l) {
+    cudaFree(d_index[l]);
+    cudaFree(d_cursor[l]);
+    cudaFreeHost(h_flush_blobs[l]);
+    d_index[l] = d_cursor[l] = nullptr;
+    h_flush_blobs[l] = nullptr;
     cudaFree(d_chunk_lut[l]);
     cudaFree(d_chunk_fixed[l]);
     cudaFree(d_gather[l]);
@@ -830,6 +851,24 @@ int Stream::kick_batch(uint32_t n_epochs, const uint32_t* epoch_masks)
     A.out = D.d_data ? D.d_data : D.data;
     D.positions = A.positions;
     D.copied = 0;
+    // the batch's runs of epochs per shard epoch, as delivery splits them
+    // (src/zarr/shard_delivery.c:105-204)
+    D.n_runs = 0;
+    for (uint32_t a = 0; a < na;) {
+      const uint32_t left = uint32_t(V.cps_append - kick_eis[l]);
+      const uint32_t run = std::min(left, na - a);
+      if (D.n_runs >= D.runs_cap)
+        return 1;
+      IndexRun& R = D.runs[D.n_runs++];
+      R.a0 = a;
+      R.run = run;
+      R.eis0 = kick_eis[l];
+      kick_eis[l] += run;
+      R.final = kick_eis[l] >= V.cps_append ? 1u : 0u;
+      if (R.final)
+        kick_eis[l] = 0;
+      a += run;
+    }
     S.level_of[S.n_levels++] = l;
   }
   // zero-copy writes handed to the sink from this slot must have retired
@@ -850,6 +889,32 @@ int Stream::kick_batch(uint32_t n_epochs, const uint32_t* epoch_masks)
   if (timed_begin(sa, &metrics.aggregate, 0, 0))
     return 1;
   CK(launch_aggregate(ab, d_agg_scratch + si * agg_scratch_slot, sa));
+  // the shard index entries of the batch and the index blobs (with their
+  // crc32c) of every shard epoch it completes
+  {
+    IndexBatch ib{};
+    ib.alignment = cfg.shard_alignment;
+    for (int k = 0; k < S.n_levels; ++k) {
+      const int l = S.level_of[k];
+      const LevelPlan& V = P.lv[l];
+      DeliverySlot::Level& D = S.lv[l];
+      IndexLevel& X = ib.lv[ib.nlevels++];
+      X.index = d_index[l];
+      X.cursor = d_cursor[l];
+      X.offsets = D.offsets;
+      X.real_sizes = D.real_sizes;
+      X.runs = D.runs;
+      X.n_runs = D.n_runs;
+      X.n_active = S.active[l];
+      X.cpi = V.cps_inner;
+      X.cps_total = V.cps_total;
+      X.shards = V.shard_inner_count;
+      X.blobs = D.blobs;
+      X.blob_bytes = blob_bytes[l];
+      ib.max_shards = std::max<uint64_t>(ib.max_shards, V.shard_inner_count);
+    }
+    CK(launch_index(ib, sa));
+  }
   // to the host: the expected bytes by the copy engine, the rest (if the
   // batch is larger: the first batch, or a less compressible one) by a
   // kernel that reads the total on the device -- no host wait either way
@@ -914,7 +979,7 @@ int Stream::deliver(int si)
     const DeliverySlot::Level& D = S.lv[l];
     const uint64_t cpi = V.cps_inner;
     Shards& SS = shards[l];
-    uint32_t a = 0;
+    uint32_t a = 0, finals = 0;
     while (a < n_active) {
       const uint32_t left = uint32_t(V.cps_append - SS.epoch_in_shard);
       const uint32_t run = std::min(left, n_active - a);
@@ -942,22 +1007,18 @@ int Stream::deliver(int si)
             return 1;
           bytes_out += wbytes;
         }
-        for (uint32_t r = 0; r < run; ++r) {
-          const uint64_t eis = SS.epoch_in_shard + r;
-          const uint64_t js = j0 + uint64_t(r) * cpi;
-          for (uint64_t j = js; j < js + cpi; ++j)
-            if (D.real_sizes[j] > 0) {
-              const uint64_t slot_idx = eis * cpi + (j - js);
-              sh.index[2 * slot_idx] = sh.cursor + (D.offsets[j] - D.offsets[j0]);
-              sh.index[2 * slot_idx + 1] = D.real_sizes[j];
-            }
-        }
         sh.cursor += wbytes;
       }
       SS.epoch_in_shard += run;
       a += run;
-      if (SS.epoch_in_shard >= V.cps_append && finalize_level(l))
-        return 1;
+      if (SS.epoch_in_shard >= V.cps_append) {
+        // the index blobs the device built for this shard epoch
+        const uint8_t* blobs =
+          D.blobs + uint64_t(finals) * V.shard_inner_count * blob_bytes[l];
+        ++finals;
+        if (write_index_blobs(l, blobs))
+          return 1;
+      }
     }
     if (sink->record_fence) {
       io_done[l] = sink->record_fence(sink, uint8_t(l));
@@ -972,35 +1033,54 @@ int Stream::deliver(int si)
   return 0;
 }
 
-// Index (u64 offset, nbytes pairs; empty = all ones) + crc32c, then finalize
-// every open shard of the level (src/zarr/shard_delivery.c:36-102).
-int Stream::finalize_level(int l)
+// Write each open shard's index blob -- zero padding to the alignment, the
+// index of (offset, nbytes) u64 pairs (all ones for an empty slot), its
+// crc32c, as the device built them -- and finalize the shards of the level
+// (src/zarr/shard_delivery.c:36-102).
+int Stream::write_index_blobs(int l, const uint8_t* blobs)
 {
-  const LevelPlan& V = P.lv[l];
   Shards& SS = shards[l];
-  const uint64_t sa = cfg.shard_alignment;
   int err = 0;
-  for (auto& sh : SS.sh) {
+  for (size_t s = 0; s < SS.sh.size(); ++s) {
+    Shard& sh = SS.sh[s];
     if (!sh.w)
       continue;
-    const uint64_t nidx = V.cps_total * 16, total = nidx + 4;
-    const uint64_t wb = sa ? round_up(total, sa) : total;
-    const uint64_t pad = wb - total;
-    std::vector<uint8_t> buf(wb, 0);
-    std::memcpy(buf.data() + pad, sh.index.data(), nidx);
-    const uint32_t crc = crc32c_host(buf.data() + pad, nidx);
-    std::memcpy(buf.data() + pad + nidx, &crc, 4);
-    if (sh.w->write(sh.w, sh.cursor, buf.data(), buf.data() + wb))
+    const uint8_t* b = blobs + s * blob_bytes[l];
+    if (sh.w->write(sh.w, sh.cursor, b, b + blob_bytes[l]))
       err = 1;
     if (sh.w->finalize(sh.w))
       err = 1;
     sh.w = nullptr;
     sh.cursor = 0;
-    std::fill(sh.index.begin(), sh.index.end(), ~uint64_t(0));
   }
   SS.epoch_in_shard = 0;
   SS.shard_epoch++;
   return err;
+}
+
+// Finalize a level's partly filled shard epoch at the flush: the device
+// writes the index blobs of its current state (and resets it).
+int Stream::finalize_level(int l)
+{
+  const LevelPlan& V = P.lv[l];
+  IndexBatch ib{};
+  ib.alignment = cfg.shard_alignment;
+  ib.nlevels = 1;
+  ib.max_shards = V.shard_inner_count;
+  IndexLevel& X = ib.lv[0];
+  X.index = d_index[l];
+  X.cursor = d_cursor[l];
+  X.cpi = V.cps_inner;
+  X.cps_total = V.cps_total;
+  X.shards = V.shard_inner_count;
+  X.blobs = h_flush_blobs[l];
+  X.blob_bytes = blob_bytes[l];
+  X.flush = 1;
+  const cudaStream_t st = agg_stream();
+  CK(launch_index(ib, st));
+  CK(cudaStreamSynchronize(st));
+  kick_eis[l] = 0;
+  return write_index_blobs(l, h_flush_blobs[l]);
 }
 
 int Stream::drain_all()
@@ -1399,10 +1479,17 @@ tile_stream_gpu_restart(tile_stream_gpu* s, shard_sink* sink)
     for (auto& sh : S.sh) {
       sh.cursor = 0;
       sh.w = nullptr;
-      std::fill(sh.index.begin(), sh.index.end(), ~uint64_t(0));
     }
+    const uint64_t ns = I.P.lv[l].shard_inner_count;
+    if (cudaMemsetAsync(I.d_index[l], 0xFF, ns * I.P.lv[l].cps_total * 16, I.s_comp) !=
+          cudaSuccess ||
+        cudaMemsetAsync(I.d_cursor[l], 0, ns * 8, I.s_comp) != cudaSuccess)
+      return 1;
+    I.kick_eis[l] = 0;
     I.io_done[l] = io_event{};
   }
+  if (cudaStreamSynchronize(I.s_comp) != cudaSuccess)
+    return 1;
   for (auto& sl : I.slot) {
     sl.busy = 0;
     for (auto& f : sl.fence)

@@ -13,8 +13,7 @@ namespace chucky {
 
 struct Shard
 {
-  uint64_t cursor = 0;         // bytes written so far
-  std::vector<uint64_t> index; // 2 * cps_total entries
+  uint64_t cursor = 0; // bytes written so far
   shard_writer* w = nullptr;
 };
 
@@ -37,6 +36,13 @@ struct DeliverySlot
     uint64_t positions_cap = 0, data_cap = 0;
     uint64_t positions = 0;         // of the batch in the slot
     uint64_t copied = 0;            // bytes already copied to the host
+    // shard index: the batch's runs of active epochs (host-written, read
+    // by the index kernel) and the final index blobs of the shard epochs
+    // the batch completes (written by the index kernel)
+    IndexRun* runs = nullptr;       // mapped
+    uint32_t n_runs = 0, runs_cap = 0;
+    uint8_t* blobs = nullptr;       // mapped [finals_cap][shards][blob_bytes]
+    uint32_t finals_cap = 0;
   };
   Level lv[LOD_MAX_LEVELS];
   uint32_t active[LOD_MAX_LEVELS] = {};
@@ -154,6 +160,13 @@ struct Stream
 
   // shards
   Shards shards[LOD_MAX_LEVELS];
+  // the shard index of the current shard epoch of every level, resident on
+  // the device, and the padded index + crc32c bytes per shard
+  uint64_t* d_index[LOD_MAX_LEVELS] = {};
+  uint64_t* d_cursor[LOD_MAX_LEVELS] = {};
+  uint64_t blob_bytes[LOD_MAX_LEVELS] = {};
+  uint8_t* h_flush_blobs[LOD_MAX_LEVELS] = {}; // mapped [shards][blob_bytes]
+  uint32_t kick_eis[LOD_MAX_LEVELS] = {}; // epoch in shard after the last kick
   io_event io_done[LOD_MAX_LEVELS] = {};
 
   // append-to-delivered latency per epoch (ms)
@@ -196,6 +209,8 @@ struct Stream
   int deliver(int si);
   int drain_all();
   int finalize_level(int l);
+  int write_index_blobs(int l, const uint8_t* blobs);
+  cudaStream_t agg_stream() const { return cfg.codec.id != CODEC_NONE ? s_agg : s_comp; }
   int flush_all();
   writer_result append(slice in);
   // Device memory appended in stream order with `producer` (a cudaStream_t

