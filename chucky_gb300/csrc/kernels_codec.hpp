@@ -34,6 +34,19 @@ struct ChunkRef
   uint64_t* size;    // compressed size (written)
 };
 
+// zstd frames back to chunk bytes (a CTA per frame, bounds-checked): frame
+// i is in_size[i] bytes at in + in_off[i] and decodes to chunk_bytes bytes
+// at out + i * out_stride; status[i] 0 when it did exactly that.
+cudaError_t launch_zstd_decode(const uint8_t* in,
+                               const uint64_t* in_off,
+                               const uint64_t* in_size,
+                               uint64_t n_chunks,
+                               uint8_t* out,
+                               uint64_t out_stride,
+                               uint64_t chunk_bytes,
+                               uint32_t* status,
+                               cudaStream_t st);
+
 struct CodecBatch
 {
   const uint8_t* in;    // first chunk (4-byte aligned)

@@ -22,6 +22,7 @@
 #include "launch.cuh"
 #include "copy.cuh"
 #include "lz77.cuh"
+#include "zstd_format.cuh"
 
 namespace chucky {
 
@@ -144,37 +145,6 @@ __device__ __forceinline__ uint32_t fse_init(const FseEnc& t, int s)
 {
   return t.states[t.first[s]] + (1u << t.al);
 }
-
-// Predefined distributions (RFC 8878 3.1.1.3.2.2).
-static const int16_t kLLNormH[36] = { 4, 3, 2, 2, 2, 2, 2, 2, 2, 2, 2, 2,
-                                     2, 1, 1, 1, 2, 2, 2, 2, 2, 2, 2, 2,
-                                     2, 3, 2, 1, 1, 1, 1, 1, -1, -1, -1, -1 };
-static const int16_t kMLNormH[53] = { 1, 4, 3, 2, 2, 2, 2, 2, 2, 1, 1, 1, 1, 1,
-                                     1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1,
-                                     1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1,
-                                     1, 1, 1, 1, -1, -1, -1, -1, -1, -1, -1 };
-static const int16_t kOFNormH[29] = { 1, 1, 1, 1, 1, 1, 2, 2, 2, 1,
-                                     1, 1, 1, 1, 1, 1, 1, 1, 1, 1,
-                                     1, 1, 1, 1, -1, -1, -1, -1, -1 };
-
-__constant__ uint32_t kLLBase[36] = { 0,  1,  2,   3,   4,   5,    6,    7,
-                                      8,  9,  10,  11,  12,  13,   14,   15,
-                                      16, 18, 20,  22,  24,  28,   32,   40,
-                                      48, 64, 128, 256, 512, 1024, 2048, 4096,
-                                      8192, 16384, 32768, 65536 };
-__constant__ uint8_t kLLBits[36] = { 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0,
-                                     0, 0, 0, 0, 1, 1, 1, 1, 2, 2, 3, 3,
-                                     4, 6, 7, 8, 9, 10, 11, 12, 13, 14, 15, 16 };
-__constant__ uint32_t kMLBase[53] = {
-  3,  4,  5,  6,  7,  8,  9,  10, 11, 12, 13, 14, 15, 16, 17, 18, 19, 20,
-  21, 22, 23, 24, 25, 26, 27, 28, 29, 30, 31, 32, 33, 34, 35, 37, 39, 41,
-  43, 47, 51, 59, 67, 83, 99, 131, 259, 515, 1027, 2051, 4099, 8195, 16387,
-  32771, 65539
-};
-__constant__ uint8_t kMLBits[53] = { 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0,
-                                     0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0,
-                                     0, 0, 0, 0, 1, 1, 1, 1, 2, 2, 3, 3, 4, 4,
-                                     5, 7, 8, 9, 10, 11, 12, 13, 14, 15, 16 };
 
 // ---------------------------------------------------------------------------
 // find

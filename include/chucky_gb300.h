@@ -157,6 +157,34 @@ extern "C"
                                uint32_t* d_status,
                                void* cuda_stream);
 
+  /* Decode zstd frames (CODEC_ZSTD chunks) on the device, for on-device
+   * verification and readback; no counterpart in the reference, which
+   * decodes with ZSTD_decompress on the host (src/cpu/compress.c:85-93).
+   * Any conforming frame (RFC 8878) decodes, not only this library's:
+   * skippable frames, several frames in a row, raw / RLE / compressed
+   * blocks, every literals and sequences mode; frames that need a
+   * dictionary are refused; a content checksum is skipped, not verified.
+   *
+   * Chunk i is d_in_sizes[i] bytes at d_in + d_in_offsets[i] and decodes to
+   * exactly `chunk_bytes` bytes at d_out + i * out_stride.  All pointers are
+   * device memory.  d_status[i] is set to 0 when chunk i decoded to exactly
+   * chunk_bytes bytes, 1 when its input ends early, 2 for an invalid field,
+   * table, bitstream or offset, 3 when it would write past chunk_bytes, 4
+   * when it decodes to fewer bytes, 5 for a dictionary frame; a malformed
+   * frame is never read or written out of bounds.  Runs asynchronously on
+   * `cuda_stream` (a cudaStream_t; NULL for the default stream); a CTA per
+   * chunk, no scratch.  Returns 0 when launched, 1 for invalid arguments, 3
+   * for a CUDA error. */
+  int chucky_zstd_decode_chunks(const void* d_in,
+                                const uint64_t* d_in_offsets,
+                                const uint64_t* d_in_sizes,
+                                size_t n_chunks,
+                                void* d_out,
+                                size_t out_stride,
+                                size_t chunk_bytes,
+                                uint32_t* d_status,
+                                void* cuda_stream);
+
 #ifdef __cplusplus
 }
 #endif

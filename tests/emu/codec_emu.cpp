@@ -9,6 +9,7 @@
 #include "../../chucky_gb300/csrc/lz4.cu"
 #include "../../chucky_gb300/csrc/lz4_decode.cu"
 #include "../../chucky_gb300/csrc/zstd.cu"
+#include "../../chucky_gb300/csrc/zstd_decode.cu"
 
 #include <dlfcn.h>
 #include <string>
@@ -20,6 +21,7 @@ void note_launches(unsigned) {}
 } // namespace chucky
 
 static uint64_t rng_state;
+static uint64_t f_of(int t, uint64_t nf) { return uint64_t(t) % nf; }
 static uint64_t rnd()
 {
   uint64_t z = (rng_state += 0x9e3779b97f4a7c15ULL);
@@ -185,6 +187,80 @@ int main(int argc, char** argv)
       return 1;
     }
     comp += sizes[c];
+  }
+  if (codec == "zstd") {
+    // the device decoder on the same frames, and on libzstd's frames of the
+    // same chunks at levels 1, 3 and 19: every chunk back exactly
+    auto zc = (size_t(*)(void*, size_t, const void*, size_t, int))dlsym(zl, "ZSTD_compress");
+    auto zb = (size_t(*)(size_t))dlsym(zl, "ZSTD_compressBound");
+    if (!zc || !zb)
+      return 3;
+    std::vector<uint8_t> frames;
+    std::vector<uint64_t> offs, lens;
+    for (uint64_t c = 0; c < n; ++c) { // ours
+      offs.push_back(frames.size());
+      lens.push_back(sizes[c]);
+      frames.insert(frames.end(), out.data() + c * out_stride,
+                    out.data() + c * out_stride + sizes[c]);
+    }
+    for (int lvl : { 1, 3, 19 })
+      for (uint64_t c = 0; c < n; ++c) {
+        std::vector<uint8_t> tmp(zb(chunk));
+        const size_t k = zc(tmp.data(), tmp.size(), flat.data() + c * chunk, chunk, lvl);
+        if (ze(k))
+          return 1;
+        offs.push_back(frames.size());
+        lens.push_back(k);
+        frames.insert(frames.end(), tmp.data(), tmp.data() + k);
+      }
+    const uint64_t nf = offs.size();
+    std::vector<uint8_t> back(nf * in_stride, 0xAB);
+    std::vector<uint32_t> st(nf, 99);
+    if (launch_zstd_decode(frames.data(), offs.data(), lens.data(), nf, back.data(),
+                           in_stride, chunk, st.data(), nullptr) != cudaSuccess)
+      return 1;
+    for (uint64_t f = 0; f < nf; ++f) {
+      const uint64_t c = f % n;
+      if (st[f] != 0 || std::memcmp(back.data() + f * in_stride, flat.data() + c * chunk, chunk)) {
+        size_t at = 0;
+        while (at < chunk && back[f * in_stride + at] == flat[c * chunk + at])
+          ++at;
+        std::fprintf(stderr, "frame %llu (%s): device zstd decoder status %u, first diff at %zu\n",
+                     (unsigned long long)f, f < n ? "ours" : "libzstd", st[f], at);
+        return 1;
+      }
+    }
+    // malformed frames (cut short, garbage, bytes flipped) report an error
+    // and stay in bounds (AddressSanitizer watches every access)
+    std::vector<uint8_t> junk(4096 + lens[0]);
+    for (auto& x : junk)
+      x = uint8_t(rnd());
+    std::vector<std::vector<uint8_t>> bad;
+    for (uint64_t cut : { uint64_t(1), uint64_t(5), lens[0] / 2, lens[0] - 1 })
+      if (cut < lens[0])
+        bad.emplace_back(frames.begin() + offs[0], frames.begin() + offs[0] + cut);
+    bad.push_back(junk);
+    for (int t = 0; t < 64; ++t) {
+      std::vector<uint8_t> b(frames.begin() + offs[f_of(t, nf)], frames.begin() + offs[f_of(t, nf)] + lens[f_of(t, nf)]);
+      b[rnd() % b.size()] ^= uint8_t(1 + rnd() % 255);
+      bad.push_back(b);
+    }
+    for (size_t t = 0; t < bad.size(); ++t) {
+      uint64_t o = 0, l = bad[t].size();
+      uint32_t s = 99;
+      std::vector<uint8_t> tmp(chunk);
+      if (launch_zstd_decode(bad[t].data(), &o, &l, 1, tmp.data(), chunk, chunk, &s, nullptr) !=
+          cudaSuccess)
+        return 1;
+      if (s > 5) {
+        std::fprintf(stderr, "malformed frame %zu: status %u\n", t, s);
+        return 1;
+      }
+      if (t < 5 && s == 0) {
+        std::fprintf(stderr, "malformed frame %zu decoded as valid\n", t);
+        return 1;
+      }
+    }
   }
   if (codec == "lz4") {
     // the device decoder on the same blocks: every chunk back exactly
