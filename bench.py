@@ -651,7 +651,7 @@ def cube_appends(lib, dev, steps):
     return out
 
 
-def encoder_roofline(lib, dev, codec="lz4", reps=5, n=64):
+def encoder_roofline(lib, dev, codec="lz4", reps=5, n=64, level=1):
     """The encoder launch set alone on one 256 MiB batch of sensor chunks
     (64 chunks of 32 x 256 x 256 u16), CUDA events on its stream: bytes
     read + written per launch set and the chunk-input rate."""
@@ -663,7 +663,7 @@ def encoder_roofline(lib, dev, codec="lz4", reps=5, n=64):
     lib.chucky_encode_bound.restype = C.c_size_t
     lib.chucky_encode_bound.argtypes = [C.c_int, C.c_size_t]
     lib.chucky_encode_scratch_bytes.restype = C.c_size_t
-    lib.chucky_encode_scratch_bytes.argtypes = [C.c_int, C.c_size_t, C.c_size_t]
+    lib.chucky_encode_scratch_bytes.argtypes = [C.c_int, C.c_int, C.c_size_t, C.c_size_t]
     cid = capi.CODEC[codec]
     frames = sensor_frames(64, dev)  # 64 frames: 2 epochs of 9 x 16 chunk tiles
     # chunk tiles 32 x 256 x 256 of the first 64 frames, as the stream lays them out
@@ -676,10 +676,9 @@ def encoder_roofline(lib, dev, codec="lz4", reps=5, n=64):
     out_stride = (bound + 15) // 16 * 16
     out = torch.empty(n * out_stride, dtype=torch.uint8, device=dev)
     sizes = torch.zeros(n, dtype=torch.int64, device=dev)
-    sb = lib.chucky_encode_scratch_bytes(cid, chunk_bytes, n)
+    sb = lib.chucky_encode_scratch_bytes(cid, level, chunk_bytes, n)
     scratch = torch.empty(sb, dtype=torch.uint8, device=dev)
     st = torch.cuda.Stream(device=dev)
-    level = 1
     times = []
     for r in range(reps + 2):
         e0 = torch.cuda.Event(enable_timing=True)
@@ -699,6 +698,7 @@ def encoder_roofline(lib, dev, codec="lz4", reps=5, n=64):
     del frames, t, chunks, pad, out, scratch
     torch.cuda.empty_cache()
     return {"input_bytes": n * chunk_bytes, "output_bytes": comp, "ms": ms,
+            "ratio": n * chunk_bytes / max(comp, 1),
             "input_gbs": n * chunk_bytes / (ms * 1e-3) / 1e9,
             "achieved_gbs": (n * chunk_bytes + comp) / (ms * 1e-3) / 1e9}
 
@@ -1038,8 +1038,10 @@ def run_single(args):
         # the encoder launch set alone on a batch of sensor chunks (48 chunks
         # of 32 x 256 x 256 u16, 192 MiB: more than L2): the ncu case
         enc = encoder_roofline(lib, torch.device("cuda"), args.single.split("-")[1],
-                               reps=args.steps, n=48)
-        print("ok", round(enc["input_gbs"], 1), flush=True)
+                               reps=args.steps, n=48,
+                               level=1 if args.level is None else args.level)
+        print("ok", round(enc["input_gbs"], 1), "GB/s ratio", round(enc["ratio"], 4),
+              flush=True)
         return
     if args.single in ("u16", "f32"):
         u16, f32 = make_cubes()
@@ -1086,6 +1088,8 @@ def main():
                                          "sensor-lz4", "encode-lz4", "encode-zstd",
                                          "served-pass"],
                     help="profiling case: one array's stream, --steps passes, no timing")
+    ap.add_argument("--level", type=int, default=None,
+                    help="codec level of --single encode-* (default 1)")
     args = ap.parse_args()
     if args.single:
         return run_single(args)

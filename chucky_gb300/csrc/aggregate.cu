@@ -93,7 +93,11 @@ agg_layout_k(AggBatch b, uint64_t* scratch, uint64_t scratch_stride)
   if (threadIdx.x == 0)
     L.offsets[L.positions] = carry;
   // the padding that rounds each shard group up to the alignment is written
-  // as zeros (no stale buffer bytes reach the shard files)
+  // as zeros (no stale buffer bytes reach the shard files), and so is the
+  // alignment's worth of bytes after the batch: a delivery write of a run
+  // of epochs is rounded up to the alignment and may read that far past
+  // the batch's last byte (src/stream/types.aggregate.c:10-26 allocates
+  // the slack, zeroed)
   if (b.alignment > 0 && L.group > 0) {
     __syncthreads();
     for (uint64_t g = 0; g < L.positions / L.group; ++g) {
@@ -103,6 +107,9 @@ agg_layout_k(AggBatch b, uint64_t* scratch, uint64_t scratch_stride)
       for (uint64_t q = beg + threadIdx.x; q < end; q += blockDim.x)
         L.out[q] = 0;
     }
+    const uint64_t total = L.offsets[L.positions];
+    for (uint64_t q = threadIdx.x; q < b.alignment; q += blockDim.x)
+      L.out[total + q] = 0;
   }
 }
 
@@ -154,7 +161,7 @@ constexpr uint64_t kTailPiece = 64 << 10;
 __global__ void __launch_bounds__(256) tail_copy_k(TailCopies t)
 {
   const TailCopy& c = t.lv[blockIdx.y];
-  const uint64_t total = *c.total;
+  const uint64_t total = *c.total + c.extra;
   if (total <= c.start)
     return;
   for (uint64_t p = c.start + blockIdx.x * kTailPiece; p < total;

@@ -403,9 +403,9 @@ int estimate_stream(const tile_stream_configuration* config,
       1, std::min<uint64_t>(nchunks, (256ull << 20) / std::max<uint64_t>(1, P.chunk_bytes)));
     uint64_t scratch = 0;
     if (config->codec.id == CODEC_ZSTD)
-      scratch = chucky::zstd_scratch_bytes(wave, uint32_t(P.chunk_bytes));
+      scratch = chucky::zstd_scratch_bytes(wave, uint32_t(P.chunk_bytes), config->codec.level);
     else if (config->codec.id == CODEC_LZ4_NON_STANDARD)
-      scratch = chucky::lz4_scratch_bytes(wave, uint32_t(P.chunk_bytes));
+      scratch = chucky::lz4_scratch_bytes(wave, uint32_t(P.chunk_bytes), config->codec.level);
     info->codec_bytes =
       2 * nchunks * 8 + (shared_encoder ? 0 : 2 * scratch); // one scratch per slot
   }

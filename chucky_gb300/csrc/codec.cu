@@ -23,8 +23,8 @@ int Stream::codec_init()
   if (wave_chunks > n)
     wave_chunks = n;
   const size_t bytes = cfg.codec.id == CODEC_ZSTD
-                         ? zstd_scratch_bytes(wave_chunks, uint32_t(P.chunk_bytes))
-                         : lz4_scratch_bytes(wave_chunks, uint32_t(P.chunk_bytes));
+                         ? zstd_scratch_bytes(wave_chunks, uint32_t(P.chunk_bytes), cfg.codec.level)
+                         : lz4_scratch_bytes(wave_chunks, uint32_t(P.chunk_bytes), cfg.codec.level);
   if (P.chunk_bytes >= (uint64_t(1) << 32))
     return 1;
   for (int i = 0; i < 2; ++i)
@@ -127,14 +127,14 @@ chucky_encode_bound(int codec_id, size_t chunk_bytes)
 }
 
 extern "C" size_t
-chucky_encode_scratch_bytes(int codec_id, size_t chunk_bytes, size_t n_chunks)
+chucky_encode_scratch_bytes(int codec_id, int level, size_t chunk_bytes, size_t n_chunks)
 {
   if (!chunk_bytes || chunk_bytes >= (size_t(1) << 32))
     return 0;
   if (codec_id == CODEC_ZSTD)
-    return chucky::zstd_scratch_bytes(n_chunks, uint32_t(chunk_bytes));
+    return chucky::zstd_scratch_bytes(n_chunks, uint32_t(chunk_bytes), level);
   if (codec_id == CODEC_LZ4_NON_STANDARD)
-    return chucky::lz4_scratch_bytes(n_chunks, uint32_t(chunk_bytes));
+    return chucky::lz4_scratch_bytes(n_chunks, uint32_t(chunk_bytes), level);
   return 0;
 }
 
@@ -159,7 +159,7 @@ chucky_encode_chunks(int codec_id,
       chunk_bytes >= (size_t(1) << 32) || in_stride < chunk_bytes ||
       (reinterpret_cast<uintptr_t>(d_chunks) & 3) || (in_stride & 3) ||
       out_stride < chucky::codec_bound(codec_id, chunk_bytes) ||
-      scratch_bytes < chucky_encode_scratch_bytes(codec_id, chunk_bytes, n_chunks)) {
+      scratch_bytes < chucky_encode_scratch_bytes(codec_id, level, chunk_bytes, n_chunks)) {
     std::fprintf(stderr, "chucky_gb300: chucky_encode_chunks: invalid arguments\n");
     return 1;
   }

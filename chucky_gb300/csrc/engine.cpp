@@ -158,8 +158,8 @@ int Engine::encode_group(Lane& L, std::vector<EncodeJob*>& group)
     total += j->n;
   const uint64_t wave = std::max<uint64_t>(
     1, std::min<uint64_t>(total, wave_bytes_ / std::max<uint32_t>(1, cb)));
-  const size_t need = first.codec == CODEC_ZSTD ? zstd_scratch_bytes(wave, cb)
-                                                : lz4_scratch_bytes(wave, cb);
+  const size_t need = first.codec == CODEC_ZSTD ? zstd_scratch_bytes(wave, cb, first.level)
+                                                : lz4_scratch_bytes(wave, cb, first.level);
   if (reserve_scratch(L, need))
     return 1;
   if (total > L.refs_cap) {

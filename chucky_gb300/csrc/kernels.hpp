@@ -182,8 +182,9 @@ cudaError_t launch_index(const IndexBatch& b, cudaStream_t st);
 struct TailCopy
 {
   uint8_t* dst;
-  const uint8_t* src; // readable 20 bytes past *total
+  const uint8_t* src; // readable 20 bytes past *total + extra
   const uint64_t* total;
+  uint64_t extra;     // bytes copied past *total (the alignment slack)
   uint64_t start;
 };
 struct TailCopies

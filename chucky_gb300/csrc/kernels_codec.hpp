@@ -111,10 +111,13 @@ struct ChunkRuns
   uint32_t slot[CodecBatch::kMaxRuns];
 };
 
-size_t lz4_scratch_bytes(uint64_t n_chunks, uint32_t chunk_bytes);
+// Scratch of one launch set.  The level selects the parse: LZ4 levels >= 2
+// and zstd levels >= 3 also search the wide window (earlier regions of the
+// chunk) and need room for its region tables.
+size_t lz4_scratch_bytes(uint64_t n_chunks, uint32_t chunk_bytes, int level);
 cudaError_t launch_lz4(CodecBatch b, void* scratch, cudaStream_t st);
 
-size_t zstd_scratch_bytes(uint64_t n_chunks, uint32_t chunk_bytes);
+size_t zstd_scratch_bytes(uint64_t n_chunks, uint32_t chunk_bytes, int level);
 cudaError_t launch_zstd(CodecBatch b, void* scratch, cudaStream_t st);
 
 } // namespace chucky

@@ -51,9 +51,19 @@ struct SegMeta
   uint32_t final_ll;  // last segment: its literal count
 };
 
+// Levels 2 and up parse with the wide window (the 3 regions before each
+// one, LZ4's 64 KiB reach); level 0 and 1 with the region's own window.
+constexpr uint32_t kLz4WideBack = 3;
+constexpr int kLz4WideLog = 15;
+__host__ __device__ inline bool lz4_wide(int level) { return level >= 2; }
+
 // One CTA per region, a warp per segment of it.
 __global__ void __launch_bounds__(32 * kSegsPerRegion)
-lz4_find_k(CodecBatch b, Seq* seqs, SegMeta* meta, uint32_t regions_per_chunk)
+lz4_find_k(CodecBatch b,
+           Seq* seqs,
+           SegMeta* meta,
+           uint32_t regions_per_chunk,
+           const uint16_t* wide_tables) // null: the region's own window only
 {
   __shared__ __align__(16) uint16_t tables[kSegsPerRegion][1 << kHashLog];
   CHUCKY_DYN_SHARED(uint32_t, words); // kRegionStageWords
@@ -78,8 +88,15 @@ lz4_find_k(CodecBatch b, Seq* seqs, SegMeta* meta, uint32_t regions_per_chunk)
       start_limit = s0;
   }
   Seq* out = seqs + seg * kMaxSeqPerSeg;
+  // the wide window: the 3 regions before (LZ4 offsets reach 65535 back)
+  const WideWindow W{ base,
+                      wide_tables ? wide_tables + chunk * regions_per_chunk *
+                                                    wide_entries(kLz4WideLog)
+                                  : nullptr,
+                      uint32_t(r0 / kRegionBytes), kLz4WideBack, 65535u, kLz4WideLog };
   const SegInfo info = lz77_parse_segment(words, r0, s0, s1, start_limit, match_end,
-                                          tables[w], out);
+                                          tables[w], out, 4,
+                                          wide_tables ? &W : nullptr);
   __syncwarp();
   // encoded size of everything but sequence 0's literal part
   uint32_t body = 0;
@@ -298,10 +315,12 @@ lz4_emit_k(CodecBatch b, const Seq* seqs, const SegMeta* meta)
 
 // Saturates at SIZE_MAX when the product would overflow, so a caller that
 // compares the result with a fixed capacity rejects absurd chunk counts.
-size_t lz4_scratch_bytes(uint64_t n_chunks, uint32_t chunk_bytes)
+size_t lz4_scratch_bytes(uint64_t n_chunks, uint32_t chunk_bytes, int level)
 {
+  const uint64_t rpc = (uint64_t(chunk_bytes) + kRegionBytes - 1) / kRegionBytes;
   const uint64_t per_chunk = ((uint64_t(chunk_bytes) + kSegBytes - 1) / kSegBytes) *
-                             (kMaxSeqPerSeg * sizeof(Seq) + sizeof(SegMeta));
+                               (kMaxSeqPerSeg * sizeof(Seq) + sizeof(SegMeta)) +
+                             (lz4_wide(level) ? rpc * wide_entries(kLz4WideLog) * 2 + 256 : 0);
   if (per_chunk && n_chunks > (SIZE_MAX - 512) / per_chunk)
     return SIZE_MAX;
   return n_chunks * per_chunk + 512;
@@ -320,9 +339,18 @@ cudaError_t launch_lz4(CodecBatch b, void* scratch, cudaStream_t st)
   SegMeta* meta = reinterpret_cast<SegMeta*>((m + 255) & ~uintptr_t(255));
   const unsigned grid = unsigned((segs + kWarps - 1) / kWarps);
   cudaError_t e;
+  uint16_t* wide = nullptr;
+  if (lz4_wide(b.level)) { // region tables after the segment metadata
+    const uintptr_t t = reinterpret_cast<uintptr_t>(meta + segs);
+    wide = reinterpret_cast<uint16_t*>((t + 255) & ~uintptr_t(255));
+    note_launches(1);
+    if ((e = lz77_launch_index(b, wide, rpc, kLz4WideLog, st)) != cudaSuccess)
+      return e;
+  }
   note_launches(3);
   CHUCKY_LAUNCH(lz4_find_k, unsigned(b.n_chunks * rpc), 32 * kSegsPerRegion,
-                kRegionStageWords * sizeof(uint32_t), st, b, seqs, meta, rpc);
+                kRegionStageWords * sizeof(uint32_t), st, b, seqs, meta, rpc,
+                static_cast<const uint16_t*>(wide));
   if ((e = cudaGetLastError()) != cudaSuccess)
     return e;
   CHUCKY_LAUNCH(lz4_plan_k, unsigned((b.n_chunks + kWarps - 1) / kWarps), 32 * kWarps, 0,

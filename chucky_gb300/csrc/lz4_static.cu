@@ -160,7 +160,7 @@ chucky_lz4_encode_chunks_static(const void* d_chunks,
                  chunk_bytes);
     return 1;
   }
-  const size_t need = chucky::lz4_scratch_bytes(n_chunks, uint32_t(chunk_bytes));
+  const size_t need = chucky::lz4_scratch_bytes(n_chunks, uint32_t(chunk_bytes), 1);
   if (need > kStaticScratchBytes) {
     std::fprintf(stderr,
                  "chucky_gb300: lz4 static encode: %zu chunks of %zu bytes need "

@@ -78,6 +78,43 @@ struct SegInfo
   uint32_t trailing; // literals after the last match of the segment
 };
 
+// ---- wide match window (the higher levels) ---------------------------------
+//
+// A region's own hash table only reaches back into the region.  At the
+// higher levels a first pass (lz77_index_k) records, for every region, the
+// last position of each hash of 4 bytes (a deterministic maximum);
+// the parse then also probes the tables of up to `back` earlier regions,
+// nearest first, verifies each candidate against the chunk in global
+// memory and takes the first that beats the lane's local match (measured
+// up to kLaneExtend - 1 bytes).
+// (hash log per codec: 15 bits for LZ4, 14 for zstd; the zstd parse reaches
+// further back, so smaller tables keep more of them in L2)
+__host__ __device__ constexpr uint64_t wide_entries(int hlog) { return uint64_t(1) << hlog; }
+// lanes whose local match is shorter than this probe the wide window
+constexpr uint32_t kWideProbeBelow = 16;
+
+struct WideWindow
+{
+  const uint8_t* chunk;   // the chunk's bytes (4-byte aligned; readable past the end)
+  const uint16_t* tables; // the chunk's region tables [regions][1 << hlog]
+  uint32_t region;        // the region being parsed
+  uint32_t back;          // earlier regions probed
+  uint32_t max_dist;      // farthest match source allowed (bytes back)
+  int hlog;               // hash bits of the tables
+};
+
+__device__ __forceinline__ uint32_t hash4w(uint32_t v, int hlog)
+{
+  return (v * 2654435761u) >> (32 - hlog);
+}
+
+// 4 bytes of `base` (4-byte aligned) at any byte position p
+__device__ __forceinline__ uint32_t load4(const uint8_t* base, uint32_t p)
+{
+  const uint32_t* w = reinterpret_cast<const uint32_t*>(base + (p & ~3u));
+  return __funnelshift_r(__ldg(w), __ldg(w + 1), (p & 3) * 8);
+}
+
 // 4 bytes at byte position `pos` of a word array.
 __device__ __forceinline__ uint32_t word_at(const uint32_t* w, uint32_t pos)
 {
@@ -144,6 +181,60 @@ __device__ __forceinline__ uint32_t lane_match(const uint32_t* words,
   return len;
 }
 
+// Candidates of a position q (region-relative, 4 bytes x) in the wide
+// window's earlier regions, nearest region first; the first that matches
+// longer than (cand, len) replaces them and ends the search.  The bytes
+// at q come from the staged region `words`, the candidate's from the chunk
+// in global memory.
+__device__ __forceinline__ void wide_probe(const WideWindow& W,
+                                           const uint32_t* words,
+                                           uint32_t r0,
+                                           uint32_t q,
+                                           uint32_t x,
+                                           uint32_t end,
+                                           bool& ok,
+                                           uint32_t& cand,
+                                           uint32_t& len)
+{
+  const uint32_t qa = r0 + q; // chunk position
+  const uint32_t h = hash4w(x, W.hlog);
+  const uint32_t cap = min(kLaneExtend - 1, end - q);
+  const uint32_t need = ok ? len + 1 : 4;
+  for (uint32_t k = 1; k <= W.back && k <= W.region; ++k) {
+    const uint32_t rr = W.region - k;
+    const uint16_t t = W.tables[uint64_t(rr) * wide_entries(W.hlog) + h];
+    if (t == 0xFFFF)
+      continue;
+    const uint32_t c = rr * kRegionBytes + t;
+    if (qa - c > W.max_dist)
+      break; // the regions further back are further still
+    if (load4(W.chunk, c) != x)
+      continue; // another value with the same hash
+    uint32_t m = 4;
+    while (m + 4 <= cap) {
+      const uint32_t d = word_at(words, q + m) ^ load4(W.chunk, c + m);
+      if (d) {
+        m += uint32_t(__ffs(int(d)) - 1) >> 3;
+        break;
+      }
+      m += 4;
+    }
+    if (m + 4 > cap) { // the last bytes before the cap, one by one
+      const uint8_t* bytes = reinterpret_cast<const uint8_t*>(words);
+      while (m < cap && bytes[q + m] == W.chunk[c + m])
+        ++m;
+    }
+    if (m > cap)
+      m = cap;
+    if (m >= need) {
+      ok = true;
+      len = m;
+      cand = c - r0; // before the region: wraps, offsets stay q - cand
+      return;
+    }
+  }
+}
+
 // Parse segment [s0, s1) of a chunk whose bytes from r0 (the region start,
 // r0 <= s0) on are staged in `words`.  Matches may start at positions in
 // [s0, start_limit), reach back to r0 and end at or before `match_end`.
@@ -157,7 +248,8 @@ __device__ inline SegInfo lz77_parse_segment(const uint32_t* words,
                                              uint32_t match_end,
                                              uint16_t* table,
                                              Seq* out,
-                                             uint32_t min_match = 4)
+                                             uint32_t min_match = 4,
+                                             const WideWindow* wide = nullptr)
 {
   const int lane = threadIdx.x & 31;
   const uint8_t* bytes = reinterpret_cast<const uint8_t*>(words);
@@ -309,8 +401,14 @@ __device__ inline SegInfo lz77_parse_segment(const uint32_t* words,
         okb = true;
       }
     }
-    const uint32_t la = oka ? lane_match(words, bytes, qa, ca, end) : 0;
-    const uint32_t lb = okb ? lane_match(words, bytes, qb, cb, end) : 0;
+    uint32_t la = oka ? lane_match(words, bytes, qa, ca, end) : 0;
+    uint32_t lb = okb ? lane_match(words, bytes, qb, cb, end) : 0;
+    if (wide) { // earlier regions, for lanes without a good local match
+      if (va && la < kWideProbeBelow)
+        wide_probe(*wide, words, r0, qa, xa, end, oka, ca, la);
+      if (vb && lb < kWideProbeBelow)
+        wide_probe(*wide, words, r0, qb, xb, end, okb, cb, lb);
+    }
     __syncwarp();
     if (va)
       table[ha] = uint16_t(qa);
@@ -446,6 +544,64 @@ __device__ inline uint32_t lz77_compact_literals(uint32_t* words,
     __syncwarp();
   }
   return out;
+}
+
+// The wide window's first pass: one CTA per region, the last position of
+// every hash of 4 bytes within the region (a maximum: the same table in
+// any thread order), written as 16-bit region offsets (0xFFFF: none).
+// `in_at(c)` gives chunk c's bytes; `rpc` regions per chunk.  The region is
+// staged and the table built in dynamic shared memory
+// (wide_index_smem(hlog) bytes).
+constexpr uint32_t kWideIndexThreads = 512;
+inline size_t wide_index_smem(int hlog)
+{
+  return size_t(wide_entries(hlog) + kRegionStageWords) * sizeof(uint32_t);
+}
+
+template<typename Batch>
+__global__ void __launch_bounds__(kWideIndexThreads)
+lz77_index_k(Batch b, uint16_t* tables, uint32_t rpc, int hlog)
+{
+  CHUCKY_DYN_SHARED(uint32_t, sm); // table, then the staged region
+  const uint32_t entries = uint32_t(wide_entries(hlog));
+  uint32_t* tbl = sm;
+  uint32_t* words = sm + entries;
+  const uint64_t chunk = blockIdx.x / rpc;
+  const uint32_t region = blockIdx.x % rpc;
+  const uint8_t* base = b.in_at(chunk);
+  const uint32_t r0 = region * kRegionBytes;
+  const uint32_t r1 = min(b.chunk_bytes, r0 + kRegionBytes);
+  uint4* t4 = reinterpret_cast<uint4*>(tbl);
+  for (uint32_t i = threadIdx.x; i < entries / 4; i += blockDim.x)
+    t4[i] = make_uint4(0, 0, 0, 0);
+  lz77_stage_region(base, r0, r1, words, threadIdx.x, blockDim.x); // (ends with a barrier)
+  // positions whose 4 bytes lie in the region
+  for (uint32_t p = threadIdx.x; p + 4 <= r1 - r0; p += blockDim.x)
+    atomicMax(&tbl[hash4w(word_at(words, p), hlog)], p + 1);
+  __syncthreads();
+  // two entries per thread and step: 4-byte stores
+  uint32_t* out = reinterpret_cast<uint32_t*>(tables + (chunk * rpc + region) * entries);
+  for (uint32_t i = threadIdx.x; i < entries / 2; i += blockDim.x) {
+    const uint32_t a = tbl[2 * i], c = tbl[2 * i + 1];
+    out[i] = (a ? a - 1 : 0xFFFFu) | ((c ? c - 1 : 0xFFFFu) << 16);
+  }
+}
+
+// Launches lz77_index_k over every region of a batch (`tables`: 4-byte
+// aligned, n_chunks * rpc * wide_entries(hlog) entries).
+template<typename Batch>
+inline cudaError_t lz77_launch_index(const Batch& b, uint16_t* tables, uint32_t rpc,
+                                     int hlog, cudaStream_t st)
+{
+  const size_t smem = wide_index_smem(hlog);
+  cudaError_t e = cudaFuncSetAttribute(lz77_index_k<Batch>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       int(smem));
+  if (e != cudaSuccess)
+    return e;
+  CHUCKY_LAUNCH(lz77_index_k<Batch>, unsigned(b.n_chunks * rpc), kWideIndexThreads, smem,
+                st, b, tables, rpc, hlog);
+  return cudaGetLastError();
 }
 
 } // namespace chucky

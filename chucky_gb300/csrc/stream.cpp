@@ -932,6 +932,7 @@ int Stream::kick_batch(uint32_t n_epochs, const uint32_t* epoch_masks)
       t.dst = D.data;
       t.src = D.d_data;
       t.total = D.offsets + D.positions; // mapped: written by the aggregation
+      t.extra = cfg.shard_alignment;     // the zeroed slack after the batch
       t.start = D.copied;
       tail_max = std::max(tail_max, D.data_cap - D.copied);
     }

@@ -90,23 +90,63 @@ __host__ __device__ __forceinline__ int highbit(uint32_t x)
 #endif
 }
 
-struct FseEnc
+// Literal-length and match-length codes (RFC 8878 3.1.1.3.2.1.1): the
+// base-value tables in closed form.
+__host__ __device__ __forceinline__ int ll_code(uint32_t ll)
+{
+  if (ll < 16)
+    return int(ll);
+  if (ll >= 64)
+    return highbit(ll) + 19;
+  if (ll < 24)
+    return 16 + int((ll - 16) >> 1);
+  if (ll < 32)
+    return 20 + int((ll - 24) >> 2);
+  if (ll < 48)
+    return 22 + int((ll - 32) >> 3);
+  return 24;
+}
+
+__host__ __device__ __forceinline__ int ml_code(uint32_t ml) // ml >= 3
+{
+  const uint32_t mb = ml - 3;
+  if (mb < 32)
+    return int(mb);
+  if (mb >= 128)
+    return highbit(mb) + 36;
+  if (mb < 40)
+    return 32 + int((mb - 32) >> 1);
+  if (mb < 48)
+    return 36 + int((mb - 40) >> 2);
+  if (mb < 64)
+    return 38 + int((mb - 48) >> 3);
+  if (mb < 96)
+    return 40 + int((mb - 64) >> 4);
+  return 42;
+}
+
+template<int kStates>
+struct FseEncT
 {
   int al;
-  int16_t count[64];  // normalized count per symbol (-1 stored as 1)
-  uint8_t first[64];  // index of the symbol's first state in `states`
-  uint8_t states[64]; // states of each symbol, ascending, grouped by symbol
+  int16_t count[64];        // normalized count per symbol (-1 stored as 1)
+  uint16_t first[64];       // index of the symbol's first state in `states`
+  uint8_t states[kStates];  // states of each symbol, ascending, grouped by symbol
 };
+using FseEnc = FseEncT<64>;  // accuracy log <= 6: Huffman weights
+using SeqEnc = FseEncT<256>; // accuracy log <= 8: sequence codes
+constexpr int kSeqMaxLog = 8;
 
 // Build encoder tables from normalized counts (-1 = "less than 1").
-// `spread` and `fill` are 64-entry scratch arrays (shared memory on the
-// device: local arrays of one thread would miss L1).
-__host__ __device__ inline void fse_build(FseEnc& t,
+// `spread` (1 << al entries) and `fill` (nsym entries) are scratch arrays
+// (shared memory on the device: local arrays of one thread would miss L1).
+template<int kStates>
+__host__ __device__ inline void fse_build(FseEncT<kStates>& t,
                                           const int16_t* norm,
                                           int nsym,
                                           int al,
                                           uint8_t* spread,
-                                          uint8_t* fill)
+                                          uint16_t* fill)
 {
   const int size = 1 << al;
   int high = size - 1;
@@ -125,7 +165,7 @@ __host__ __device__ inline void fse_build(FseEnc& t,
   int acc = 0;
   for (int s = 0; s < nsym; ++s) {
     t.count[s] = norm[s] == -1 ? 1 : norm[s];
-    t.first[s] = uint8_t(acc);
+    t.first[s] = uint16_t(acc);
     acc += t.count[s];
   }
   for (int s = 0; s < nsym; ++s)
@@ -138,10 +178,11 @@ __host__ __device__ inline void fse_build(FseEnc& t,
 // The three predefined sequence tables, built once on the host.
 struct PredefTables
 {
-  FseEnc ll, ml, of;
+  SeqEnc ll, ml, of;
 };
 
-__device__ __forceinline__ uint32_t fse_init(const FseEnc& t, int s)
+template<int kStates>
+__device__ __forceinline__ uint32_t fse_init(const FseEncT<kStates>& t, int s)
 {
   return t.states[t.first[s]] + (1u << t.al);
 }
@@ -155,15 +196,35 @@ __device__ __forceinline__ uint32_t fse_init(const FseEnc& t, int s)
 // (kSegBytes each), adds them to its chunk's literal histogram
 // (`chunk_hist`, kHistWords per chunk, zeroed before the launch) and
 // records whether its input and its literals are single-valued.
+// Levels 3 and up parse with the wide window (the 7 regions before each
+// one: matches up to 112-128 KiB back) and accept matches from
+// kMinMatchWide bytes; levels below with the region's own window.
+constexpr uint32_t kZstdWideBack = 7;
+constexpr int kZstdWideLog = 14;
+#ifndef CHUCKY_ZSTD_MIN_MATCH_WIDE
+#define CHUCKY_ZSTD_MIN_MATCH_WIDE 4
+#endif
+constexpr uint32_t kMinMatchWide = CHUCKY_ZSTD_MIN_MATCH_WIDE;
+__host__ __device__ inline bool zstd_wide(int level) { return level >= 3; }
+// Per-chunk counts of the sequence codes (levels with the wide window):
+// LL codes at 0, ML codes at kSeqHistML, OF codes at kSeqHistOF; a word
+// set when a sequence cannot be coded.
+constexpr uint32_t kSeqHistML = 36, kSeqHistOF = 36 + 53, kSeqHistBad = 36 + 53 + 32;
+constexpr uint32_t kSeqHistWords = 128;
+
 __global__ void __launch_bounds__(32 * kSegsPerRegion)
 zstd_find_k(CodecBatch b,
             Seq* seqs,
             ZSeg* meta,
             uint32_t* chunk_hist,
             uint8_t* litbuf,
-            uint32_t regions_per_chunk)
+            uint32_t regions_per_chunk,
+            const uint16_t* wide_tables, // null: the region's own window only
+            uint32_t* seq_hist)          // null: no sequence-code histograms
 {
   __shared__ __align__(16) uint16_t tables[kSegsPerRegion][1 << kHashLog];
+  __shared__ uint32_t seg_nseq[kSegsPerRegion], seg_trail[kSegsPerRegion];
+  __shared__ uint32_t shist[kSeqHistWords];
   CHUCKY_DYN_SHARED(uint32_t, words); // kRegionStageWords
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint64_t chunk = blockIdx.x / regions_per_chunk;
@@ -177,9 +238,54 @@ zstd_find_k(CodecBatch b,
   const uint64_t seg = chunk * b.segs_per_chunk + s0 / kSegBytes;
   Seq* out = seqs + (has ? seg : 0) * kMaxSeqPerSeg;
   SegInfo info{ 0, 0 };
-  if (has)
-    info = lz77_parse_segment(words, r0, s0, s1, s1, s1, tables[w], out, kMinMatch);
+  if (has) {
+    const WideWindow W{ base,
+                        wide_tables ? wide_tables + chunk * regions_per_chunk *
+                                                      wide_entries(kZstdWideLog)
+                                    : nullptr,
+                        uint32_t(r0 / kRegionBytes), kZstdWideBack,
+                        (kZstdWideBack + 1) * kRegionBytes, kZstdWideLog };
+    info = lz77_parse_segment(words, r0, s0, s1, s1, s1, tables[w], out,
+                              wide_tables ? kMinMatchWide : kMinMatch,
+                              wide_tables ? &W : nullptr);
+  }
+  if (lane == 0) {
+    seg_nseq[w] = info.nseq;
+    seg_trail[w] = info.trailing;
+  }
+  if (seq_hist)
+    for (int i = threadIdx.x; i < int(kSeqHistWords); i += blockDim.x)
+      shist[i] = 0;
   __syncthreads(); // the region is no longer needed as history
+  if (seq_hist && has) {
+    // codes of the segment's sequences (as the block kernel forms them:
+    // the first takes the literals carried from the block's earlier
+    // segments since its last sequence), counted per CTA
+    uint32_t carry = 0;
+    for (int k = w - w % int(kSegsPerBlock); k < w; ++k)
+      carry = seg_nseq[k] ? seg_trail[k] : carry + seg_trail[k];
+    for (uint32_t i0 = 0; i0 < info.nseq; i0 += 32) {
+      const uint32_t i = i0 + lane;
+      const bool v = i < info.nseq;
+      unsigned code[3] = { ~0u, ~0u, ~0u };
+      if (v) {
+        const Seq x = out[i];
+        const uint32_t ll = x.lit + (i == 0 ? carry : 0), ml = x.match, off = x.offset + 3;
+        const int oc = highbit(off);
+        if (oc > 28 || ml < 3 || off <= 3)
+          shist[kSeqHistBad] = 1;
+        code[0] = unsigned(ll_code(ll));
+        code[1] = kSeqHistML + unsigned(ml < 3 ? 0 : ml_code(ml));
+        code[2] = kSeqHistOF + unsigned(oc);
+      }
+#pragma unroll
+      for (int t = 0; t < 3; ++t) { // lanes past the sequences carry ~0u
+        const unsigned peers = __match_any_sync(0xffffffffu, code[t]);
+        if (v && lane == __ffs(int(peers)) - 1)
+          atomicAdd(&shist[code[t]], uint32_t(__popc(peers)));
+      }
+    }
+  }
   uint32_t* bitmap = reinterpret_cast<uint32_t*>(tables[w]);
   uint32_t* hist = bitmap + (kSegBytes / 32 + 31) / 32 * 32; // after the bitmap
   uint32_t* pres = hist + 256;
@@ -269,6 +375,14 @@ zstd_find_k(CodecBatch b,
         atomicOr(ch + i, t);
     }
   }
+  if (seq_hist) // the CTA's code counts, added to its chunk's
+    for (int i = threadIdx.x; i < int(kSeqHistWords); i += blockDim.x)
+      if (shist[i]) {
+        if (i == int(kSeqHistBad))
+          seq_hist[chunk * kSeqHistWords + i] = 1;
+        else
+          atomicAdd(seq_hist + chunk * kSeqHistWords + i, shist[i]);
+      }
 }
 
 // ---------------------------------------------------------------------------
@@ -491,7 +605,9 @@ struct TableShared
 struct BlockShared
 {
   uint32_t cl[256];                   // the chunk's Huffman codes
-  PredefTables pre;                   // predefined sequence tables
+  PredefTables seqt;                  // the chunk's sequence tables (LL, ML, OF)
+  uint32_t seq_modes;                 // modes byte of a block with sequences
+  uint32_t seq_desc;                  // description bytes after it (carrier)
   uint32_t seg_nseq[kSegsPerBlock];
   uint32_t seg_seq0[kSegsPerBlock];   // block index of the segment's first sequence
   uint32_t seg_carry[kSegsPerBlock];
@@ -566,31 +682,6 @@ struct BitPack
   }
 };
 
-__device__ __forceinline__ int ll_code_s(uint32_t ll, const uint32_t* base)
-{
-  if (ll < 16)
-    return int(ll);
-  if (ll >= 64)
-    return highbit(ll) + 19;
-  int c = 16; // 16..63
-  while (c < 35 && base[c + 1] <= ll)
-    ++c;
-  return c;
-}
-
-__device__ __forceinline__ int ml_code_s(uint32_t ml, const uint32_t* base)
-{
-  const uint32_t mb = ml - 3;
-  if (mb < 32)
-    return int(mb);
-  if (mb >= 128)
-    return highbit(mb) + 36;
-  int c = 32;
-  while (c < 52 && base[c + 1] <= ml)
-    ++c;
-  return c;
-}
-
 // Literal length (with the carry into a segment's first sequence), match
 // length and offset value (offset + 3, no repeat offsets) of block
 // sequence j.
@@ -614,8 +705,9 @@ __device__ __forceinline__ void seq_at(const BlockShared& S,
 }
 
 // Low bits of FSE state u (v = u + table size) when encoding `sym`.
-template<typename F>
-__device__ __forceinline__ int state_bits(const FseEnc& t, uint32_t u, int sym, F& put)
+template<int kStates, typename F>
+__device__ __forceinline__ int state_bits(const FseEncT<kStates>& t, uint32_t u, int sym,
+                                          F& put)
 {
   const uint32_t v = u + (1u << t.al);
   const int c = t.count[sym];
@@ -642,13 +734,13 @@ __device__ __forceinline__ uint32_t seq_emit(const BlockShared& S,
 {
   uint32_t ll, ml, off;
   seq_at(S, seqs, segbase, nsegs, j, ll, ml, off);
-  const int lc = ll_code_s(ll, S.ll_base), mc = ml_code_s(ml, S.ml_base);
+  const int lc = ll_code(ll), mc = ml_code(ml);
   const int oc = highbit(off);
   uint32_t bits = 0;
   if (j + 1 < nseq) {
-    bits += state_bits(S.pre.of, st[2 * nseq + j], oc, put);
-    bits += state_bits(S.pre.ml, st[nseq + j], mc, put);
-    bits += state_bits(S.pre.ll, st[j], lc, put);
+    bits += state_bits(S.seqt.of, st[2 * nseq + j], oc, put);
+    bits += state_bits(S.seqt.ml, st[nseq + j], mc, put);
+    bits += state_bits(S.seqt.ll, st[j], lc, put);
   }
   const int lb = S.ll_bits[lc], mb = S.ml_bits[mc];
   put(ll - S.ll_base[lc], lb);
@@ -1136,6 +1228,189 @@ zstd_table_k(CodecBatch b,
   }
 }
 
+// ---- adaptive sequence tables (levels with the wide window) ---------------
+//
+// The wide window's parse yields many short matches whose codes are far from
+// the predefined distributions.  A CTA per chunk counts the chunk's
+// literal-length, match-length and offset codes and normalizes each
+// histogram into an FSE table (RFC 8878 4.1.1) wherever that beats the
+// predefined table, description included.  The chunk's first block with
+// sequences that is not an RLE block (the carrier, never replaced by a raw
+// block) describes the tables (FSE_Compressed mode); every later block
+// refers to them (Repeat mode).  A repeated table is the one of the previous
+// compressed block with sequences, which is the carrier or a block that
+// repeated it.
+
+struct ChunkSeq
+{
+  SeqEnc t[3];          // LL, ML, OF encoders
+  uint8_t desc[3][96];  // descriptions of the described tables (LL, ML, OF)
+  uint32_t desc_len[3];
+  uint32_t mode[3];     // 0 predefined, 2 described by the carrier
+  uint32_t carrier;     // block describing the tables; ~0u: none
+};
+
+struct SeqTabShared
+{
+  uint32_t hist[kSeqHistWords];
+  uint32_t carrier;
+  int16_t norm[3][64];
+  uint8_t spread[3][256];
+  uint16_t fill[3][64];
+  ChunkSeq cs;
+};
+
+// Normalize counts to 2^al (al large enough that 2^al >= 2 nsym): every
+// present symbol >= 1, no "less than 1" symbols; a lone symbol shares the
+// table with an absent one, so that no table is single-valued.  nsym >= 2.
+__device__ void norm_seq(const uint32_t* hist, int nsym, int al, int16_t* norm)
+{
+  const int size = 1 << al;
+  uint64_t total = 0;
+  int present = 0, only = 0;
+  for (int s = 0; s < nsym; ++s) {
+    total += hist[s];
+    if (hist[s]) {
+      ++present;
+      only = s;
+    }
+  }
+  int sum = 0;
+  for (int s = 0; s < nsym; ++s) {
+    int c = 0;
+    if (hist[s]) {
+      c = int((uint64_t(hist[s]) * uint64_t(size) + total / 2) / total);
+      c = c < 1 ? 1 : c;
+    }
+    norm[s] = int16_t(c);
+    sum += c;
+  }
+  if (present == 1) {
+    for (int s = 0; s < nsym; ++s)
+      norm[s] = 0;
+    norm[only] = int16_t(size - 1);
+    norm[only == 0 ? 1 : 0] = 1;
+    return;
+  }
+  while (sum > size) { // take from the largest
+    int best = -1;
+    for (int s = 0; s < nsym; ++s)
+      if (norm[s] > 1 && (best < 0 || norm[s] > norm[best]))
+        best = s;
+    norm[best]--;
+    --sum;
+  }
+  while (sum < size) { // give to the most under-represented
+    int best = -1;
+    for (int s = 0; s < nsym; ++s)
+      if (hist[s] && (best < 0 || uint64_t(hist[s]) * uint64_t(norm[best]) >
+                                    uint64_t(hist[best]) * uint64_t(norm[s])))
+        best = s;
+    norm[best]++;
+    ++sum;
+  }
+}
+
+// Coded bits of a histogram under normalized counts of accuracy log al
+// (a count of -1 codes like 1).
+__device__ float fse_cost(const uint32_t* hist, int nhist, const int16_t* norm, int nsym,
+                          int al)
+{
+  float c = 0.f;
+  for (int s = 0; s < nhist; ++s)
+    if (hist[s]) {
+      if (s >= nsym)
+        return 3.0e38f;
+      const int n = norm[s] < 1 ? 1 : norm[s];
+      c += float(hist[s]) * (float(al) - log2f(float(n)));
+    }
+  return c;
+}
+
+__global__ void __launch_bounds__(kTableThreads)
+zstd_seqtab_k(CodecBatch b,
+              const ZSeg* meta,
+              const uint32_t* seq_hist,
+              ChunkSeq* out,
+              uint32_t blocks_per_chunk)
+{
+  __shared__ SeqTabShared T;
+  const int tid = threadIdx.x;
+  const uint64_t chunk = blockIdx.x;
+  for (int i = tid; i < int(kSeqHistWords); i += blockDim.x)
+    T.hist[i] = seq_hist[chunk * kSeqHistWords + i];
+  if (tid == 0)
+    T.carrier = ~0u;
+  __syncthreads();
+  // the carrier: the first block with sequences that is not an RLE block
+  // (its segments' records, as the block kernel reads them)
+  const uint64_t seg_first = chunk * b.segs_per_chunk;
+  for (uint32_t bi = tid; bi < blocks_per_chunk; bi += blockDim.x) {
+    const uint32_t b0 = bi * kBlockBytes;
+    const uint32_t b1 = min(b.chunk_bytes, b0 + kBlockBytes);
+    const uint32_t nsegs = (b1 - b0 + kSegBytes - 1) / kSegBytes;
+    const uint64_t sb = seg_first + b0 / kSegBytes;
+    const uint32_t in0 = (meta[sb].flags >> 16) & 0xFF;
+    uint32_t nseq = 0, all_same = 1;
+    for (uint32_t k = 0; k < nsegs; ++k) {
+      const ZSeg m = meta[sb + k];
+      all_same &= (m.flags >> 24) & (((m.flags >> 16) & 0xFF) == in0);
+      nseq += m.nseq;
+    }
+    if (nseq && !all_same)
+      atomicMin(&T.carrier, bi);
+  }
+  __syncthreads();
+  if (tid < 3) { // a thread per table
+    const int t = tid;
+    const int nhist = t == 0 ? 36 : (t == 1 ? 53 : 32);
+    const int pre_n = t == 0 ? 36 : (t == 1 ? 53 : 29);
+    const int pre_al = t == 2 ? 5 : 6;
+    const int16_t* pre = t == 0 ? kLLNormD : (t == 1 ? kMLNormD : kOFNormD);
+    const uint32_t* h = T.hist + (t == 0 ? 0 : (t == 1 ? kSeqHistML : kSeqHistOF));
+    uint64_t total = 0;
+    int last = -1;
+    for (int s = 0; s < nhist; ++s) {
+      total += h[s];
+      if (h[s])
+        last = s;
+    }
+    SeqEnc& e = T.cs.t[t];
+    uint32_t mode = 0;
+    if (!T.hist[kSeqHistBad] && T.carrier != ~0u && last >= 0) {
+      const int nsym = last + 1 > 2 ? last + 1 : 2;
+      const uint32_t tot32 = total > 0xFFFFFFFFull ? 0xFFFFFFFFu : uint32_t(total);
+      int al = tot32 > 32 ? highbit(tot32) - 2 : 5;
+      const int lo = highbit(uint32_t(nsym - 1)) + 2;
+      al = al < lo ? lo : al;
+      al = al < 5 ? 5 : (al > kSeqMaxLog ? kSeqMaxLog : al);
+      norm_seq(h, nsym, al, T.norm[t]);
+      const int dl = write_ncount(T.cs.desc[t], T.norm[t], nsym, al);
+      const float custom = fse_cost(h, nhist, T.norm[t], nsym, al) + 8.f * float(dl);
+      const float predefined = fse_cost(h, nhist, pre, pre_n, pre_al);
+      if (custom + 32.f < predefined) {
+        mode = 2;
+        fse_build(e, T.norm[t], nsym, al, T.spread[t], T.fill[t]);
+        T.cs.desc_len[t] = uint32_t(dl);
+      }
+    }
+    if (mode == 0) {
+      fse_build(e, pre, pre_n, pre_al, T.spread[t], T.fill[t]);
+      T.cs.desc_len[t] = 0;
+    }
+    T.cs.mode[t] = mode;
+  }
+  __syncthreads();
+  if (tid == 0)
+    T.cs.carrier = T.cs.mode[0] | T.cs.mode[1] | T.cs.mode[2] ? T.carrier : ~0u;
+  __syncthreads();
+  static_assert(sizeof(ChunkSeq) % 4 == 0, "word copy");
+  const uint32_t* src = reinterpret_cast<const uint32_t*>(&T.cs);
+  uint32_t* dst = reinterpret_cast<uint32_t*>(out + chunk);
+  for (int i = tid; i < int(sizeof(ChunkSeq) / 4); i += blockDim.x)
+    dst[i] = src[i];
+}
+
 // 12 CTAs per SM (40 registers, a few spilled): the block kernel waits at
 // its phase barriers, and more resident CTAs cover those waits (measured
 // 3 % faster on the cube workload than 8 CTAs with 64 registers)
@@ -1148,6 +1423,7 @@ zstd_block_k(CodecBatch b,
              const Seq* seqs,
              const ZSeg* meta,
              const ChunkTable* tables,
+             const ChunkSeq* cseq, // adaptive sequence tables; null: predefined
              const uint8_t* litbuf,
              uint8_t* stage_all,
              uint32_t* block_sizes,
@@ -1171,12 +1447,31 @@ zstd_block_k(CodecBatch b,
   const ChunkTable& ct = tables[chunk];
   for (int c = tid; c < 256; c += blockDim.x)
     S.cl[c] = ct.cl[c];
-  // the three predefined sequence tables (built once on the host)
+  // the three sequence tables: the chunk's (adaptive) or the predefined
+  // ones (built once on the host)
   {
-    const uint32_t* src = reinterpret_cast<const uint32_t*>(&pre);
-    uint32_t* dst = reinterpret_cast<uint32_t*>(&S.pre);
+    static_assert(sizeof(PredefTables) == 3 * sizeof(SeqEnc), "LL, ML, OF in a row");
+    const uint32_t* src = cseq ? reinterpret_cast<const uint32_t*>(cseq[chunk].t)
+                               : reinterpret_cast<const uint32_t*>(&pre);
+    uint32_t* dst = reinterpret_cast<uint32_t*>(&S.seqt);
     for (int i = tid; i < int(sizeof(PredefTables) / 4); i += blockDim.x)
       dst[i] = src[i];
+  }
+  if (tid == 0) {
+    // modes byte (LL, OF, ML in bits 7-6, 5-4, 3-2): a described table is
+    // FSE_Compressed in the carrier and Repeat after it
+    uint32_t modes = 0, desc = 0;
+    if (cseq && cseq[chunk].carrier != ~0u) {
+      const ChunkSeq& c = cseq[chunk];
+      const bool carrier = bi == c.carrier;
+      const uint32_t m = carrier ? 2u : 3u;
+      modes = (c.mode[0] ? m << 6 : 0u) | (c.mode[2] ? m << 4 : 0u) |
+              (c.mode[1] ? m << 2 : 0u);
+      if (carrier)
+        desc = c.desc_len[0] + c.desc_len[1] + c.desc_len[2];
+    }
+    S.seq_modes = modes;
+    S.seq_desc = desc;
   }
   for (int i = tid; i < 53; i += blockDim.x) {
     S.ml_base[i] = kMLBase[i];
@@ -1260,6 +1555,9 @@ zstd_block_k(CodecBatch b,
         S.forced = bi == ct.carrier;
       }
     }
+    // the block describing the chunk's sequence tables stays compressed too
+    if (S.seq_desc)
+      S.forced = 1;
   }
   __syncthreads();
 
@@ -1481,13 +1779,13 @@ zstd_block_k(CodecBatch b,
     const int oc = highbit(off);
     if (oc > 28 || ml < 3 || off <= 3)
       S.seq_bad = 1;
-    scode[j] = uint8_t(ll_code_s(ll, S.ll_base));
-    scode[nseq + j] = uint8_t(ml_code_s(ml, S.ml_base));
+    scode[j] = uint8_t(ll_code(ll));
+    scode[nseq + j] = uint8_t(ml < 3 ? 0 : ml_code(ml));
     scode[2 * nseq + j] = uint8_t(oc);
   }
   __syncthreads();
   if (warp == 0 && lane < 3 && nseq) {
-    const FseEnc& t = lane == 0 ? S.pre.ll : (lane == 1 ? S.pre.ml : S.pre.of);
+    const SeqEnc& t = lane == 0 ? S.seqt.ll : (lane == 1 ? S.seqt.ml : S.seqt.of);
     uint8_t* a = scode + lane * nseq;
     const uint32_t size = 1u << t.al;
     uint32_t v = t.states[t.first[a[nseq - 1]]] + size;
@@ -1527,12 +1825,15 @@ zstd_block_k(CodecBatch b,
       before += S.warp_bits[w];
     total_bits += S.warp_bits[w];
   }
-  // header: sequence count, then the modes byte (predefined tables)
+  // header: sequence count, then the modes byte and (carrier) the table
+  // descriptions
   const uint32_t seq_at0 = 3 + S.lit_size;
-  const uint32_t nhdr = nseq == 0 ? 1 : (nseq < 128 ? 2 : (nseq < 0x7F00 ? 3 : 4));
+  const uint32_t nhdr =
+    nseq == 0 ? 1 : (nseq < 128 ? 2 : (nseq < 0x7F00 ? 3 : 4)) + S.seq_desc;
   const uint32_t bs0 = seq_at0 + nhdr; // first byte of the bitstream
-  // 17 bits of final states and the end mark
-  const uint32_t nbytes = nseq ? (total_bits + 17 + 1 + 7) / 8 : 0;
+  // final states and the end mark
+  const uint32_t fin_bits = uint32_t(S.seqt.ll.al + S.seqt.ml.al + S.seqt.of.al);
+  const uint32_t nbytes = nseq ? (total_bits + fin_bits + 1 + 7) / 8 : 0;
   const bool fits = bs0 + nbytes + 4 <= kStageBytes && !S.seq_bad;
   if (fits) {
     if (tid == 0) {
@@ -1547,8 +1848,16 @@ zstd_block_k(CodecBatch b,
         put_le(o, nseq - 0x7F00, 2);
         o += 2;
       }
-      if (nseq)
-        *o = 0; // predefined LL, OF and ML tables
+      if (nseq) {
+        *o++ = uint8_t(S.seq_modes);
+        if (S.seq_desc) { // descriptions in the order LL, OF, ML
+          const ChunkSeq& c = cseq[chunk];
+          const int order[3] = { 0, 2, 1 };
+          for (int k = 0; k < 3; ++k)
+            for (uint32_t i = 0; i < c.desc_len[order[k]]; ++i)
+              *o++ = c.desc[order[k]][i];
+        }
+      }
     }
     const uint32_t z1 = bs0 + nbytes + 4;
     const uint32_t v0 = min(z1, (bs0 + 15) & ~15u), v1 = max(v0, z1 & ~15u);
@@ -1568,9 +1877,9 @@ zstd_block_k(CodecBatch b,
       seq_emit(S, seqs, segbase, nsegs, nseq, scode, nseq - 1 - p,
                [&](uint32_t v, int n) { bp.put(v, n); });
     if (p1 == nseq && p1 > p0) { // the stream's last sequence: states, end mark
-      bp.put(S.final_state[1], 6);
-      bp.put(S.final_state[2], 5);
-      bp.put(S.final_state[0], 6);
+      bp.put(S.final_state[1], S.seqt.ml.al);
+      bp.put(S.final_state[2], S.seqt.of.al);
+      bp.put(S.final_state[0], S.seqt.ll.al);
       bp.put(1, 1);
     }
     bp.flush();
@@ -1664,14 +1973,23 @@ zstd_frame_k(CodecBatch b,
 
 } // namespace
 
-size_t zstd_scratch_bytes(uint64_t n_chunks, uint32_t chunk_bytes)
+size_t zstd_scratch_bytes(uint64_t n_chunks, uint32_t chunk_bytes, int level)
 {
+  const uint64_t wide =
+    zstd_wide(level)
+      ? n_chunks * ((uint64_t(chunk_bytes) + kRegionBytes - 1) / kRegionBytes) *
+            wide_entries(kZstdWideLog) * 2 + 256
+      : 0;
   const uint64_t segs = n_chunks * ((chunk_bytes + kSegBytes - 1) / kSegBytes);
   const uint64_t blocks =
     n_chunks * ((chunk_bytes + kBlockBytes - 1) / kBlockBytes);
+  const uint64_t adaptive =
+    zstd_wide(level) ? n_chunks * (sizeof(ChunkSeq) + kSeqHistWords * sizeof(uint32_t)) + 256
+                     : 0;
   return segs * (kMaxSeqPerSeg * sizeof(Seq) + sizeof(ZSeg) + kSegBytes) +
          blocks * (kStageBytes + sizeof(uint32_t)) +
-         n_chunks * (kHistWords * sizeof(uint32_t) + sizeof(ChunkTable)) + 2048;
+         n_chunks * (kHistWords * sizeof(uint32_t) + sizeof(ChunkTable)) + 2048 + wide +
+         adaptive;
 }
 
 cudaError_t launch_zstd(CodecBatch b, void* scratch, cudaStream_t st)
@@ -1699,20 +2017,39 @@ cudaError_t launch_zstd(CodecBatch b, void* scratch, cudaStream_t st)
   p += b.n_chunks * sizeof(ChunkTable);
   p = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(p) + 255) & ~uintptr_t(255));
   uint8_t* litbuf = p; // segs * kSegBytes, read up to 20 bytes past a slot
+  p += segs * kSegBytes + 64;
   const uint32_t rpc = (b.chunk_bytes + kRegionBytes - 1) / kRegionBytes;
   cudaError_t e;
   if ((e = cudaMemsetAsync(hist, 0, b.n_chunks * kHistWords * sizeof(uint32_t), st)) !=
       cudaSuccess)
     return e;
+  uint16_t* wide = nullptr;
+  ChunkSeq* cseq = nullptr;
+  uint32_t* seq_hist = nullptr;
+  if (zstd_wide(b.level)) { // region tables of the wide window, sequence tables
+    wide = reinterpret_cast<uint16_t*>((reinterpret_cast<uintptr_t>(p) + 255) &
+                                       ~uintptr_t(255));
+    const uintptr_t c = reinterpret_cast<uintptr_t>(wide + uint64_t(b.n_chunks) * rpc *
+                                                             wide_entries(kZstdWideLog));
+    cseq = reinterpret_cast<ChunkSeq*>((c + 255) & ~uintptr_t(255));
+    seq_hist = reinterpret_cast<uint32_t*>(cseq + b.n_chunks);
+    if ((e = cudaMemsetAsync(seq_hist, 0, b.n_chunks * kSeqHistWords * sizeof(uint32_t),
+                             st)) != cudaSuccess)
+      return e;
+    note_launches(1);
+    if ((e = lz77_launch_index(b, wide, rpc, kZstdWideLog, st)) != cudaSuccess)
+      return e;
+  }
   note_launches(4);
   CHUCKY_LAUNCH(zstd_find_k, unsigned(b.n_chunks * rpc), 32 * kSegsPerRegion,
                 kRegionStageWords * sizeof(uint32_t), st, b, seqs, meta, hist, litbuf,
-                rpc);
+                rpc, static_cast<const uint16_t*>(wide), seq_hist);
   if ((e = cudaGetLastError()) != cudaSuccess)
     return e;
   static const PredefTables pre = [] {
     PredefTables t{};
-    uint8_t spread[64], fill[64];
+    uint8_t spread[64];
+    uint16_t fill[64];
     fse_build(t.ll, kLLNormH, 36, 6, spread, fill);
     fse_build(t.ml, kMLNormH, 53, 6, spread, fill);
     fse_build(t.of, kOFNormH, 29, 5, spread, fill);
@@ -1722,8 +2059,16 @@ cudaError_t launch_zstd(CodecBatch b, void* scratch, cudaStream_t st)
                 tables, bpc);
   if ((e = cudaGetLastError()) != cudaSuccess)
     return e;
+  if (cseq) {
+    note_launches(1);
+    CHUCKY_LAUNCH(zstd_seqtab_k, unsigned(b.n_chunks), kTableThreads, 0, st, b, meta,
+                  static_cast<const uint32_t*>(seq_hist), cseq, bpc);
+    if ((e = cudaGetLastError()) != cudaSuccess)
+      return e;
+  }
   CHUCKY_LAUNCH(zstd_block_k, unsigned(blocks), kBlockThreads, kBlockBytes + 16, st, b,
-                pre, seqs, meta, tables, litbuf, stage, bsizes, bpc);
+                pre, seqs, meta, tables, static_cast<const ChunkSeq*>(cseq), litbuf, stage,
+                bsizes, bpc);
   if ((e = cudaGetLastError()) != cudaSuccess)
     return e;
   CHUCKY_LAUNCH(zstd_frame_k, unsigned(blocks), 256, 0, st, b, stage, bsizes, bpc);

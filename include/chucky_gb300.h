@@ -106,7 +106,9 @@ extern "C"
    *
    * chucky_encode_bound: worst-case encoded size of one chunk (0 for a
    * codec other than CODEC_LZ4_NON_STANDARD / CODEC_ZSTD).
-   * chucky_encode_scratch_bytes: device scratch chucky_encode_chunks needs.
+   * chucky_encode_scratch_bytes: device scratch chucky_encode_chunks needs
+   * (the level matters: LZ4 levels >= 2 and zstd levels >= 3 search a
+   * wider window, with region tables of about the input's size).
    * chucky_encode_chunks: encodes `n_chunks` chunks of `chunk_bytes`, chunk
    * i at d_chunks + i * in_stride (device memory, 4-byte aligned, the 256
    * bytes after the last chunk readable), into raw LZ4 blocks or zstd
@@ -117,7 +119,7 @@ extern "C"
    * writes for the same chunk bytes.  Returns 0, 1 for invalid arguments,
    * 3 for a CUDA error. */
   size_t chucky_encode_bound(int codec_id, size_t chunk_bytes);
-  size_t chucky_encode_scratch_bytes(int codec_id, size_t chunk_bytes,
+  size_t chucky_encode_scratch_bytes(int codec_id, int level, size_t chunk_bytes,
                                      size_t n_chunks);
   int chucky_encode_chunks(int codec_id,
                            int level,

@@ -4,6 +4,7 @@
 // available, so out-of-bounds and misaligned accesses abort with a report.
 //
 // usage: codec_emu <lz4|zstd> <chunk_bytes> <n_chunks> <pattern> <seed>
+//                  [refs] [level=<n>]
 #include "simt.hpp"
 
 #include "../../chucky_gb300/csrc/lz4.cu"
@@ -113,6 +114,15 @@ int main(int argc, char** argv)
   const uint64_t n = std::stoull(argv[3]);
   const std::string pat = argv[4];
   rng_state = std::stoull(argv[5]);
+  bool refs_mode = false;
+  int level = 1;
+  for (int a = 6; a < argc; ++a) {
+    const std::string opt = argv[a];
+    if (opt == "refs")
+      refs_mode = true;
+    else if (opt.rfind("level=", 0) == 0)
+      level = std::stoi(opt.substr(6));
+  }
   const uint64_t in_stride = (chunk + 255) / 256 * 256;
   const uint64_t bound = codec == "zstd"
                            ? chunk + (chunk >> 8) + (chunk < (128u << 10) ? ((128u << 10) - chunk) >> 11 : 0)
@@ -132,9 +142,9 @@ int main(int argc, char** argv)
   b.out = out.data();
   b.out_stride = out_stride;
   b.out_sizes = sizes.data();
-  b.level = 1;
-  const size_t sb = codec == "zstd" ? zstd_scratch_bytes(n, chunk)
-                                    : lz4_scratch_bytes(n, chunk);
+  b.level = level;
+  const size_t sb = codec == "zstd" ? zstd_scratch_bytes(n, chunk, level)
+                                    : lz4_scratch_bytes(n, chunk, level);
   std::vector<uint8_t> scratch(sb);
   const cudaError_t e = codec == "zstd" ? launch_zstd(b, scratch.data(), nullptr)
                                         : launch_lz4(b, scratch.data(), nullptr);
@@ -303,7 +313,7 @@ int main(int argc, char** argv)
       }
     }
   }
-  if (argc > 6 && std::string(argv[6]) == "refs") {
+  if (refs_mode) {
     // The same chunks addressed one by one (CodecBatch::refs, as the shared
     // encoder engine gathers several streams' chunks): chunks in reverse
     // order in a buffer of another stride, outputs and sizes in reverse
@@ -325,7 +335,7 @@ int main(int argc, char** argv)
     CodecBatch rb{};
     rb.chunk_bytes = chunk;
     rb.n_chunks = n;
-    rb.level = 1;
+    rb.level = level;
     rb.refs = refs.data();
     std::vector<uint8_t> scratch2(sb, 0x5A);
     if ((codec == "zstd" ? launch_zstd(rb, scratch2.data(), nullptr)
@@ -351,7 +361,7 @@ int main(int argc, char** argv)
       }
     }
   }
-  std::printf("ok %s chunk=%u n=%llu pattern=%s ratio=%.3f\n", codec.c_str(), chunk,
-              (unsigned long long)n, pat.c_str(), double(n * chunk) / double(comp));
+  std::printf("ok %s chunk=%u n=%llu pattern=%s level=%d ratio=%.3f\n", codec.c_str(), chunk,
+              (unsigned long long)n, pat.c_str(), level, double(n * chunk) / double(comp));
   return 0;
 }

@@ -20,6 +20,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <functional>
+#include <math.h>
 #include <thread>
 #include <vector>
 

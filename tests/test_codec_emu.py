@@ -46,30 +46,83 @@ BIG = [("zstd", "xor16", 200000, 1), ("zstd", "mixed", 131072, 2),
        ("lz4", "halves", 300000, 2), ("lz4", "random", 270000, 1)]
 
 
-def _run(emu, codec, pattern, chunk, n, *extra):
-    r = subprocess.run([emu, codec, str(chunk), str(n), pattern, "7", *extra],
-                       capture_output=True, text=True, timeout=600)
+# The higher levels: the wide match window (region tables of earlier regions
+# probed by the parse) and, for zstd, FSE-described sequence tables in the
+# chunk's first block with sequences, repeated by every later block.
+WIDE = [("lz4", "xor16", 40000, 1, 2), ("lz4", "mixed", 65536, 2, 2),
+        ("lz4", "halves", 70000, 2, 2), ("lz4", "geom", 9000, 1, 2),
+        ("zstd", "xor16", 40000, 1, 3), ("zstd", "mixed", 131072, 2, 3),
+        ("zstd", "geom", 20000, 1, 3), ("zstd", "u200", 70000, 1, 3),
+        ("zstd", "halves", 70000, 2, 3)]
+WIDE_SMALL = [(1024, 6), (37, 3), (1, 2)]
+REFS = [("zstd", "mixed", 70000, 3), ("lz4", "mixed", 70000, 3),
+        ("zstd", "xor16", 1024, 5), ("lz4", "random", 37, 4)]
+
+
+def _key(codec, pattern, chunk, n, *extra):
+    return (codec, str(chunk), str(n), pattern) + tuple(extra)
+
+
+def _cases():
+    """Every emulator run of this module (they are independent processes,
+    run side by side by the `runs` fixture)."""
+    keys = [_key(*c) for c in BIG]
+    keys += [_key(c, p, ch, n) for c in ("lz4", "zstd")
+             for p in ("zeros", "random", "ramp", "mixed", "xor16") for ch, n in CASES]
+    keys += [_key(c, p, ch, n, "level=%d" % lv) for c, p, ch, n, lv in WIDE]
+    keys += [_key(c, p, ch, n, "level=%d" % lv) for c, lv in (("lz4", 2), ("zstd", 3))
+             for p in ("zeros", "mixed", "xor16") for ch, n in WIDE_SMALL]
+    keys += [_key(c, p, ch, n, "refs", lv) for c, p, ch, n in REFS
+             for lv in ("level=1", "level=3")]
+    return keys
+
+
+@pytest.fixture(scope="module")
+def runs(emu):
+    from concurrent.futures import ThreadPoolExecutor
+
+    def one(k):
+        codec, chunk, n, pattern = k[:4]
+        return k, subprocess.run([emu, codec, chunk, n, pattern, "7", *k[4:]],
+                                 capture_output=True, text=True, timeout=900)
+
+    with ThreadPoolExecutor(max_workers=max(1, os.cpu_count() or 1)) as ex:
+        return dict(ex.map(one, _cases()))
+
+
+def _run(runs, codec, pattern, chunk, n, *extra):
+    r = runs[_key(codec, pattern, chunk, n, *extra)]
     assert r.returncode == 0, r.stderr[-2000:]
     assert r.stdout.startswith("ok")
 
 
 @pytest.mark.parametrize("codec,pattern,chunk,n", BIG)
-def test_encoder_multi_block_chunks(emu, codec, pattern, chunk, n):
-    _run(emu, codec, pattern, chunk, n)
+def test_encoder_multi_block_chunks(runs, codec, pattern, chunk, n):
+    _run(runs, codec, pattern, chunk, n)
 
 
 @pytest.mark.parametrize("codec", ["lz4", "zstd"])
 @pytest.mark.parametrize("pattern", ["zeros", "random", "ramp", "mixed", "xor16"])
 @pytest.mark.parametrize("chunk,n", CASES)
-def test_encoder_decodes_with_stock_library(emu, codec, pattern, chunk, n):
-    _run(emu, codec, pattern, chunk, n)
+def test_encoder_decodes_with_stock_library(runs, codec, pattern, chunk, n):
+    _run(runs, codec, pattern, chunk, n)
 
 
-@pytest.mark.parametrize("codec,pattern,chunk,n", [("zstd", "mixed", 70000, 3),
-                                                  ("lz4", "mixed", 70000, 3),
-                                                  ("zstd", "xor16", 1024, 5),
-                                                  ("lz4", "random", 37, 4)])
-def test_encoder_per_chunk_references(emu, codec, pattern, chunk, n):
+@pytest.mark.parametrize("codec,pattern,chunk,n,level", WIDE)
+def test_wide_window_levels(runs, codec, pattern, chunk, n, level):
+    _run(runs, codec, pattern, chunk, n, "level=%d" % level)
+
+
+@pytest.mark.parametrize("codec,level", [("lz4", 2), ("zstd", 3)])
+@pytest.mark.parametrize("pattern", ["zeros", "mixed", "xor16"])
+@pytest.mark.parametrize("chunk,n", WIDE_SMALL)
+def test_wide_window_small_chunks(runs, codec, level, pattern, chunk, n):
+    _run(runs, codec, pattern, chunk, n, "level=%d" % level)
+
+
+@pytest.mark.parametrize("codec,pattern,chunk,n", REFS)
+@pytest.mark.parametrize("level", ["level=1", "level=3"])
+def test_encoder_per_chunk_references(runs, codec, pattern, chunk, n, level):
     """Chunks addressed through a per-chunk reference list (the shared
     encoder engine's batches) decode to their bytes."""
-    _run(emu, codec, pattern, chunk, n, "refs")
+    _run(runs, codec, pattern, chunk, n, "refs", level)

@@ -35,7 +35,7 @@ def _data(kind, dtype, n, seed):
     return out
 
 
-@pytest.mark.parametrize("codec,level", [("lz4", 1), ("zstd", 1), ("zstd", 3)])
+@pytest.mark.parametrize("codec,level", [("lz4", 1), ("lz4", 2), ("zstd", 1), ("zstd", 3)])
 @pytest.mark.parametrize("name", CODEC_CASES)
 @pytest.mark.parametrize("kind", ["mixed", "random", "zeros", "ramp"])
 def test_gpu_chunks_decode_to_oracle_bytes(codec, level, name, kind):

@@ -122,7 +122,7 @@ def _zstd_lib():
     lib.chucky_encode_bound.restype = C.c_size_t
     lib.chucky_encode_bound.argtypes = [C.c_int, C.c_size_t]
     lib.chucky_encode_scratch_bytes.restype = C.c_size_t
-    lib.chucky_encode_scratch_bytes.argtypes = [C.c_int, C.c_size_t, C.c_size_t]
+    lib.chucky_encode_scratch_bytes.argtypes = [C.c_int, C.c_int, C.c_size_t, C.c_size_t]
     return lib
 
 
@@ -160,7 +160,10 @@ def _zstd_compress(x, level):
     return buf.raw[:k]
 
 
-def test_zstd_decodes_own_encoder_output():
+@pytest.mark.parametrize("level", [1, 3])
+def test_zstd_decodes_own_encoder_output(level):
+    """Level 3 frames carry FSE-described sequence tables in the first
+    block with sequences and repeat them in later blocks."""
     import torch
     lib = _zstd_lib()
     n, chunk = 16, 200000  # several 8 KiB zstd blocks and Huffman streams per chunk
@@ -171,12 +174,12 @@ def test_zstd_decodes_own_encoder_output():
     stride = (bound + 15) // 16 * 16
     d_out = torch.empty(n * stride, dtype=torch.uint8, device="cuda")
     d_sizes = torch.zeros(n, dtype=torch.int64, device="cuda")
-    sb = lib.chucky_encode_scratch_bytes(2, chunk, n)
+    sb = lib.chucky_encode_scratch_bytes(2, level, chunk, n)
     scratch = torch.empty(sb, dtype=torch.uint8, device="cuda")
     s = C.c_void_p(torch.cuda.current_stream().cuda_stream)
-    assert lib.chucky_encode_chunks(2, 1, d_in.data_ptr(), chunk, chunk, n, d_out.data_ptr(),
-                                    stride, d_sizes.data_ptr(), scratch.data_ptr(), sb,
-                                    s) == 0
+    assert lib.chucky_encode_chunks(2, level, d_in.data_ptr(), chunk, chunk, n,
+                                    d_out.data_ptr(), stride, d_sizes.data_ptr(),
+                                    scratch.data_ptr(), sb, s) == 0
     torch.cuda.synchronize()
     sizes = d_sizes.cpu().numpy().tolist()
     raw = d_out.cpu().numpy()
