@@ -709,6 +709,101 @@ def encoder_roofline(lib, dev, codec="lz4", reps=5, n=64, level=1):
 LZ4_SENSOR_TRAFFIC_PER_INPUT_BYTE = (209.0 + 268.5 + 527.8 + 144.2) / 201.3
 
 
+def _stock_codecs():
+    """liblz4 / libzstd, the reference CPU path's codecs
+    (src/cpu/compress.c:55-93: LZ4_compress_HC and ZSTD_compress at the
+    configured level)."""
+    z = C.CDLL("libzstd.so.1")
+    z.ZSTD_compressBound.restype = C.c_size_t
+    z.ZSTD_compressBound.argtypes = [C.c_size_t]
+    z.ZSTD_compress.restype = C.c_size_t
+    z.ZSTD_compress.argtypes = [C.c_void_p, C.c_size_t, C.c_void_p, C.c_size_t, C.c_int]
+    z.ZSTD_isError.argtypes = [C.c_size_t]
+    l4 = C.CDLL("liblz4.so.1")
+    l4.LZ4_compressBound.argtypes = [C.c_int]
+    l4.LZ4_compress_HC.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int]
+
+    def zstd(x, level):
+        cap = z.ZSTD_compressBound(len(x))
+        buf = C.create_string_buffer(cap)
+        k = z.ZSTD_compress(buf, cap, x, len(x), level)
+        if z.ZSTD_isError(k):
+            raise RuntimeError("ZSTD_compress failed")
+        return k
+
+    def lz4hc(x, level):
+        cap = l4.LZ4_compressBound(len(x))
+        buf = C.create_string_buffer(cap)
+        k = l4.LZ4_compress_HC(x, buf, len(x), cap, level)
+        if k <= 0:
+            raise RuntimeError("LZ4_compress_HC failed")
+        return k
+    return zstd, lz4hc
+
+
+def codec_ratios(lib, dev):
+    """Compressed bytes of the 256^3 cubes' level-0 chunks (64^3, the
+    multiscale and cube workloads' chunking) from this library's device
+    encoders and from the reference CPU path's codecs at the same level:
+    zstd-3 on the u16 and f32 cubes (the multiscale workload's codec), LZ4
+    at levels 1 and 2 on the u16 cube (the cube workload's codec)."""
+    import torch
+    f = lib.chucky_encode_chunks
+    f.restype = C.c_int
+    f.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_size_t, C.c_size_t, C.c_size_t,
+                  C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p]
+    lib.chucky_encode_bound.restype = C.c_size_t
+    lib.chucky_encode_bound.argtypes = [C.c_int, C.c_size_t]
+    lib.chucky_encode_scratch_bytes.restype = C.c_size_t
+    lib.chucky_encode_scratch_bytes.argtypes = [C.c_int, C.c_int, C.c_size_t, C.c_size_t]
+    zstd, lz4hc = _stock_codecs()
+    u16, f32 = make_cubes()
+    n = (SIDE // CHUNK) ** 3
+
+    def tiles(a):
+        t = a.reshape(SIDE // CHUNK, CHUNK, SIDE // CHUNK, CHUNK, SIDE // CHUNK, CHUNK)
+        return np.ascontiguousarray(t.transpose(0, 2, 4, 1, 3, 5)).reshape(n, -1).view(np.uint8)
+
+    def gpu_bytes(chunks, codec, level):
+        cb = chunks.shape[1]
+        cid = capi.CODEC[codec]
+        d_in = torch.zeros(n * cb + 256, dtype=torch.uint8, device=dev)
+        d_in[: n * cb] = torch.from_numpy(chunks.reshape(-1)).to(dev)
+        stride = (lib.chucky_encode_bound(cid, cb) + 15) // 16 * 16
+        out = torch.empty(n * stride, dtype=torch.uint8, device=dev)
+        sizes = torch.zeros(n, dtype=torch.int64, device=dev)
+        sb = lib.chucky_encode_scratch_bytes(cid, level, cb, n)
+        scratch = torch.empty(sb, dtype=torch.uint8, device=dev)
+        st = torch.cuda.current_stream(dev)
+        if f(cid, level, d_in.data_ptr(), cb, cb, n, out.data_ptr(), stride,
+             sizes.data_ptr(), scratch.data_ptr(), sb, st.cuda_stream):
+            raise RuntimeError("chucky_encode_chunks failed")
+        torch.cuda.synchronize(dev)
+        return int(sizes.sum().item())
+
+    def entry(chunks, codec, level, cpu):
+        raw = chunks.size
+        g = gpu_bytes(chunks, codec, level)
+        c = sum(cpu(chunks[i].tobytes(), level) for i in range(n))
+        return {"level": level, "input_bytes": int(raw), "gpu_bytes": g, "cpu_bytes": int(c),
+                "gpu_ratio": round(raw / g, 4), "cpu_ratio": round(raw / c, 4),
+                "gpu_over_cpu_bytes": round(g / c, 4)}
+
+    t16, t32 = tiles(u16), tiles(f32)
+    z16, z32 = entry(t16, "zstd", 3, zstd), entry(t32, "zstd", 3, zstd)
+    both = {k: z16[k] + z32[k] for k in ("input_bytes", "gpu_bytes", "cpu_bytes")}
+    return {
+        "chunks": "the 256^3 cubes' 64 level-0 chunks of 64^3 each",
+        "cpu_codec": "libzstd ZSTD_compress / liblz4 LZ4_compress_HC (the reference "
+                     "CPU path's codecs) at the same level",
+        "multiscale_zstd3": {"u16": z16, "f32": z32,
+                             "both_gpu_over_cpu_bytes": round(both["gpu_bytes"] /
+                                                              both["cpu_bytes"], 4)},
+        "cube_lz4": {"level1": entry(t16, "lz4", 1, lz4hc),
+                     "level2": entry(t16, "lz4", 2, lz4hc)},
+    }
+
+
 def run_served_bench(args, rank, world):
     import torch
     import chucky_gb300 as cg
@@ -760,6 +855,7 @@ def run_served_bench(args, rank, world):
     cube = cube_appends(lib, dev, max(3, args.steps // 2))
     enc = encoder_roofline(lib, dev, "lz4")
     enc_z = encoder_roofline(lib, dev, "zstd")
+    ratios = codec_ratios(lib, dev) if rank == 0 else None
 
     totals = max_over_ranks([float(np.sum(ms_dev)), float(np.sum(ms_host)),
                              float(np.sum(pms_dev)), float(np.sum(pms_host))], world, dev)
@@ -807,6 +903,7 @@ def run_served_bench(args, rank, world):
             "engine_rounds", "engine_jobs", "engine_launch_sets",
             "engine_max_jobs_per_round")},
         "compression_ratio": round(nbytes / max(1.0, out_b), 4),
+        "codec_ratios": ratios,
         "orca_e2e": orca,
         "cube_appends": cube,
         "roofline": {"kernel": "lz4 encoder launch set (find+plan+emit) on 64 sensor "
