@@ -804,6 +804,21 @@ def codec_ratios(lib, dev):
     }
 
 
+def autotune_table(lib):
+    """The encoder autotuner's choices in this process (key -> parameters)."""
+    lib.chucky_autotune_enabled.restype = C.c_int
+    names = {v: k for k, v in capi.CODEC.items()}
+    out = []
+    for e in capi.autotune_entries(lib):
+        out.append({"codec": names.get(e.codec, e.codec), "level": e.level,
+                    "dtype": capi.DTYPES[e.dtype], "chunk": list(e.chunk_shape[:e.rank]),
+                    "strength": e.strength or "default",
+                    "min_match": e.min_match or "default",
+                    "sample_gbs": round(e.encode_gbs, 1), "sample_ratio": round(e.ratio, 4),
+                    "candidates": e.candidates})
+    return {"enabled": bool(lib.chucky_autotune_enabled()), "entries": out}
+
+
 def run_served_bench(args, rank, world):
     import torch
     import chucky_gb300 as cg
@@ -828,7 +843,7 @@ def run_served_bench(args, rank, world):
     clocks = Clocks()
     # the served form: one server (start-up: a resident stream per request),
     # device-input passes, host-input passes, then the paced latency pass
-    with serve.Server(48 << 30, 16, True) as srv:
+    with serve.Server(48 << 30, 16, True, autotune=args.autotune) as srv:
         srv.prewarm(host_reqs, sink, per_request=True)
         if rank == 0:
             clocks.start()
@@ -842,11 +857,12 @@ def run_served_bench(args, rank, world):
         lat_ms = _server_pass(srv, host_reqs, sink, paced=True)
         lat = srv.stats()
     # the plain form: one request at a time, each stream encoding on its own
-    with serve.Server(1 << 62, 1, False) as psrv:
+    with serve.Server(1 << 62, 1, False, autotune=args.autotune) as psrv:
         psrv.prewarm(host_reqs, sink, per_request=False)
         pms_dev, _, _ = timed_passes(psrv, dev_reqs, lib, sink, args.steps, args.warmup)
         pms_host, _, _ = timed_passes(psrv, host_reqs, lib, sink, args.steps,
                                       max(1, args.warmup // 2))
+    tune = autotune_table(lib)
     link = h2d_probe([r.data for r in host_reqs[:4]], [r.data for r in dev_reqs[:4]], dev)
     lib.chucky_discard_sink_destroy(sink)
     del dev_reqs
@@ -898,6 +914,7 @@ def run_served_bench(args, rank, world):
                                 "0.5 ms; pinned host inputs",
                     "definition": "append of an epoch's last byte to the end of the "
                                   "sink writes of its batch"},
+        "autotune": tune,
         "served_stats": {k: st_dev[k] for k in (
             "peak_open", "peak_resident_bytes", "streams_created", "streams_reused",
             "engine_rounds", "engine_jobs", "engine_launch_sets",
@@ -1123,7 +1140,7 @@ def run_single(args):
                 on_dev[id(r.data)] = r.data.to(dev)
         reqs = [dataclasses.replace(r, data=on_dev[id(r.data)], _cfg=None) for r in host]
         sink = slib.chucky_discard_sink_create()
-        with serve.Server(48 << 30, 16, True) as srv:
+        with serve.Server(48 << 30, 16, True, autotune=args.autotune) as srv:
             srv.prewarm(reqs, sink, per_request=True)
             for _ in range(1 + args.steps):
                 srv.replay(reqs, sink, paced=False)
@@ -1187,6 +1204,9 @@ def main():
                     help="profiling case: one array's stream, --steps passes, no timing")
     ap.add_argument("--level", type=int, default=None,
                     help="codec level of --single encode-* (default 1)")
+    ap.add_argument("--autotune", type=int, default=1, choices=[0, 1],
+                    help="served form: encoder autotuner on (1, default) or off (0); "
+                         "the plain form of the same run uses the same choice")
     args = ap.parse_args()
     if args.single:
         return run_single(args)

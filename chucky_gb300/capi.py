@@ -206,7 +206,26 @@ def bind_zarr_fs_sink(lib):
 class ServerConfig(C.Structure):
     _fields_ = [("hbm_budget_bytes", C.c_size_t), ("max_streams", C.c_int),
                 ("batch_encoders", C.c_int), ("encoder_wave_bytes", C.c_size_t),
-                ("encoder_lanes", C.c_int)]
+                ("encoder_lanes", C.c_int), ("autotune", C.c_int)]
+
+
+class AutotuneEntry(C.Structure):
+    """struct chucky_autotune_entry (include/chucky_gb300.h)."""
+    _fields_ = [("codec", C.c_int), ("level", C.c_int), ("dtype", C.c_int),
+                ("rank", C.c_int), ("chunk_shape", C.c_uint64 * 16),
+                ("chunk_bytes", C.c_uint64), ("strength", C.c_int),
+                ("min_match", C.c_int), ("encode_gbs", C.c_double),
+                ("ratio", C.c_double), ("candidates", C.c_uint32)]
+
+
+def autotune_entries(lib):
+    """The encoder autotuner's table (a list of AutotuneEntry)."""
+    lib.chucky_autotune_entries.restype = C.c_size_t
+    lib.chucky_autotune_entries.argtypes = [C.c_void_p, C.c_size_t]
+    n = lib.chucky_autotune_entries(None, 0)
+    arr = (AutotuneEntry * max(1, n))()
+    lib.chucky_autotune_entries(arr, n)
+    return list(arr)[:n]
 
 
 class ServerStats(C.Structure):

@@ -16,6 +16,13 @@ int Stream::codec_init()
     return 0;
   if (cfg.codec.id != CODEC_LZ4_NON_STANDARD && cfg.codec.id != CODEC_ZSTD)
     return 1;
+  tune_key = TuneKey{};
+  tune_key.codec = cfg.codec.id;
+  tune_key.level = cfg.codec.level;
+  tune_key.dtype = int(cfg.dtype);
+  tune_key.rank = cfg.rank;
+  for (int d = 0; d < cfg.rank && d < 16; ++d)
+    tune_key.chunk[d] = cfg.dimensions[d].chunk_size;
   // The encoders' scratch grows with their input; batches larger than
   // kWaveBytes are encoded in waves that reuse one scratch area.
   constexpr uint64_t kWaveBytes = 256ull << 20;
@@ -63,6 +70,8 @@ int Stream::codec_compress(const uint8_t* pool,
     b.n_chunks = n;
     b.out_stride = comp_stride;
     b.level = cfg.codec.level;
+    b.strength = tune.strength;
+    b.min_match = tune.min_match;
     if (d_ids) { // chunk slots listed explicitly
       b.in = pool;
       b.out = out;

@@ -126,7 +126,8 @@ int Engine::reserve_scratch(Lane& L, size_t bytes)
 }
 
 // One round: every job waits for its inputs on the lane's stream, then each
-// (codec, level, chunk bytes) group is encoded as one batch, then every
+// (codec, level, parse parameters, chunk bytes) group is encoded as one
+// batch, then every
 // job's `done` event is recorded.
 int Engine::process(std::vector<EncodeJob*>& jobs)
 {
@@ -137,10 +138,11 @@ int Engine::process(std::vector<EncodeJob*>& jobs)
     if (j->out_free)
       ECK(cudaStreamWaitEvent(L.st, j->out_free, 0));
   }
-  std::map<std::tuple<int, int, uint32_t>, std::vector<EncodeJob*>> groups;
+  std::map<std::tuple<int, int, int, int, uint32_t>, std::vector<EncodeJob*>> groups;
   for (EncodeJob* j : jobs)
     if (j->n)
-      groups[std::make_tuple(j->codec, j->level, j->chunk_bytes)].push_back(j);
+      groups[std::make_tuple(j->codec, j->level, j->strength, j->min_match,
+                             j->chunk_bytes)].push_back(j);
   for (auto& g : groups)
     if (encode_group(L, g.second))
       return 1;
@@ -203,6 +205,8 @@ int Engine::encode_group(Lane& L, std::vector<EncodeJob*>& group)
     b.chunk_bytes = cb;
     b.n_chunks = std::min<uint64_t>(wave, total - f);
     b.level = first.level;
+    b.strength = first.strength;
+    b.min_match = first.min_match;
     b.refs = L.d_refs + f;
     const cudaError_t e = first.codec == CODEC_ZSTD ? launch_zstd(b, L.scratch, L.st)
                                                     : launch_lz4(b, L.scratch, L.st);

@@ -6,7 +6,7 @@
 // the compressed chunks and sizes go, the event that says its chunk pool is
 // filled) and waits until the engine has enqueued the job's encoders.  The
 // engine thread takes every job queued at that moment, groups them by
-// (codec, chunk bytes) and encodes each group as one batch over a list of
+// (codec, level, parse parameters, chunk bytes) and encodes each group as one batch over a list of
 // per-chunk addresses (CodecBatch::refs) -- one launch set for the chunks
 // of all streams, in waves of at most `wave_bytes` of input -- on one of
 // two engine CUDA streams (consecutive rounds alternate, so they overlap on
@@ -35,6 +35,7 @@ struct EncodeJob
 {
   int codec = 0;             // CODEC_LZ4_NON_STANDARD or CODEC_ZSTD
   int level = 0;
+  int strength = 0, min_match = 0; // parse parameters (CodecBatch)
   uint32_t chunk_bytes = 0;  // codec input per chunk
   const uint8_t* pool = nullptr; // chunk slot s at pool + s * in_stride
   uint64_t in_stride = 0;

@@ -58,6 +58,12 @@ struct CodecBatch
   uint64_t* out_sizes;  // [n_chunks] compressed sizes (written)
   uint32_t segs_per_chunk;
   int level;
+  // parse parameters (0: the level's defaults), e.g. chosen by the
+  // autotuner: search strength (positions probed per lane step grow by one
+  // for every 2^strength literals since the last match) and the shortest
+  // match taken (LZ4 >= 4; zstd levels without the wide window)
+  int strength;
+  int min_match;
   const uint32_t* chunk_ids; // optional: encode only these chunk slots
   // Otherwise, optionally, the slots as runs of consecutive slots (a batch
   // whose levels are not all active): entry id_base + i lies in run r when

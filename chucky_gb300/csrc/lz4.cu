@@ -94,9 +94,10 @@ lz4_find_k(CodecBatch b,
                                                     wide_entries(kLz4WideLog)
                                   : nullptr,
                       uint32_t(r0 / kRegionBytes), kLz4WideBack, 65535u, kLz4WideLog };
-  const SegInfo info = lz77_parse_segment(words, r0, s0, s1, start_limit, match_end,
-                                          tables[w], out, 4,
-                                          wide_tables ? &W : nullptr);
+  const SegInfo info = lz77_parse_segment(
+    words, r0, s0, s1, start_limit, match_end, tables[w], out,
+    b.min_match > 4 ? uint32_t(b.min_match) : 4u, wide_tables ? &W : nullptr,
+    b.strength > 0 ? b.strength : kSearchStrength);
   __syncwarp();
   // encoded size of everything but sequence 0's literal part
   uint32_t body = 0;

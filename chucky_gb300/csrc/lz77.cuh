@@ -52,8 +52,9 @@ constexpr uint32_t kLaneExtend = 64;
 #ifndef CHUCKY_HISTORY_SEGS
 #define CHUCKY_HISTORY_SEGS 1
 #endif
-// positions probed per lane step grow by one for every 2^kSearchStrength
-// literals since the last match (sparse probing of incompressible runs)
+// positions probed per lane step grow by one for every 2^strength literals
+// since the last match (sparse probing of incompressible runs); the default
+// strength (a batch may carry another, CodecBatch::strength)
 constexpr int kSearchStrength = CHUCKY_SEARCH_STRENGTH;
 // segments of the region before a warp's own that enter its table, and the
 // stride of the positions entered
@@ -249,7 +250,8 @@ __device__ inline SegInfo lz77_parse_segment(const uint32_t* words,
                                              uint16_t* table,
                                              Seq* out,
                                              uint32_t min_match = 4,
-                                             const WideWindow* wide = nullptr)
+                                             const WideWindow* wide = nullptr,
+                                             int strength = kSearchStrength)
 {
   const int lane = threadIdx.x & 31;
   const uint8_t* bytes = reinterpret_cast<const uint8_t*>(words);
@@ -358,7 +360,7 @@ __device__ inline SegInfo lz77_parse_segment(const uint32_t* words,
   // not see a's positions in the table (b finds them only as runs or short
   // periods), in exchange for twice the independent work per step.
   while (w0 < lim) {
-    const uint32_t step = 1 + ((w0 > lit_start ? w0 - lit_start : 0) >> kSearchStrength);
+    const uint32_t step = 1 + ((w0 > lit_start ? w0 - lit_start : 0) >> strength);
     const uint32_t qa = w0 + lane * step, qb = qa + 32 * step;
     const bool va = qa < lim && qa + 4 <= end, vb = qb < lim && qb + 4 <= end;
     uint32_t xa = 0, xb = 0, ha = 0, hb = 0, ca = 0, cb = 0;

@@ -3,6 +3,7 @@
 // engine, and a request-loop driver.
 #include "chucky_serve.h"
 #include "chucky_gb300.h"
+#include "autotune.hpp"
 #include "engine.hpp"
 #include "stream_internal.hpp"
 
@@ -117,6 +118,8 @@ chucky_server_create(const chucky_server_config* config)
     delete s;
     return nullptr;
   }
+  if (config->autotune)
+    chucky::autotune_set_enabled(true);
   if (config->batch_encoders) {
     s->engine.reset(new (std::nothrow) chucky::Engine());
     const uint64_t wave = config->encoder_wave_bytes ? config->encoder_wave_bytes

@@ -752,6 +752,19 @@ int Stream::kick_batch(uint32_t n_epochs, const uint32_t* epoch_masks)
             ids[n++] = uint32_t(base + j);
         }
     runs.first[runs.n] = uint32_t(n);
+    if (!tuned) {
+      // the autotuner (when on) picks this key's encoder parameters on up
+      // to 16 chunks spread over the first batch
+      if (autotune_enabled() && n) {
+        const uint8_t* sample[16];
+        const uint32_t k = uint32_t(std::min<uint64_t>(16, n));
+        const uint64_t slot_bytes = layout.chunk_stride * P.bpe;
+        for (uint32_t i = 0; i < k; ++i)
+          sample[i] = comp + uint64_t(ids[uint64_t(i) * n / k]) * slot_bytes;
+        tune = autotune(tune_key, uint32_t(P.chunk_bytes), sample, k, ev_pool_ready);
+      }
+      tuned = true;
+    }
     const uint32_t* d_ids = nullptr;
     const ChunkRuns* rp = nullptr;
     if (n != nchunks) {
@@ -775,6 +788,8 @@ int Stream::kick_batch(uint32_t n_epochs, const uint32_t* epoch_masks)
       J = EncodeJob{};
       J.codec = cfg.codec.id;
       J.level = cfg.codec.level;
+      J.strength = tune.strength;
+      J.min_match = tune.min_match;
       J.chunk_bytes = uint32_t(P.chunk_bytes);
       J.pool = comp;
       J.in_stride = layout.chunk_stride * P.bpe;

@@ -1,6 +1,7 @@
 // Internal state of one GPU stream (not part of the C ABI).
 #pragma once
 
+#include "autotune.hpp"
 #include "engine.hpp"
 #include "kernels.hpp"
 #include "plan.hpp"
@@ -114,6 +115,11 @@ struct Stream
   Engine* engine = nullptr;
   EncodeJob job[2];
   cudaEvent_t ev_engine_done[2] = {};
+  // encoder parameters: the autotuner's for this stream's key (chosen at
+  // the first batch when tuning is on), else the level's defaults
+  TuneKey tune_key{};
+  TuneParams tune{};
+  bool tuned = false;
 
   // transpose
   uint64_t* d_row_off = nullptr;

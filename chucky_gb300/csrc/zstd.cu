@@ -245,9 +245,11 @@ zstd_find_k(CodecBatch b,
                                     : nullptr,
                         uint32_t(r0 / kRegionBytes), kZstdWideBack,
                         (kZstdWideBack + 1) * kRegionBytes, kZstdWideLog };
-    info = lz77_parse_segment(words, r0, s0, s1, s1, s1, tables[w], out,
-                              wide_tables ? kMinMatchWide : kMinMatch,
-                              wide_tables ? &W : nullptr);
+    const uint32_t mm = wide_tables ? kMinMatchWide
+                                    : (b.min_match >= 4 ? uint32_t(b.min_match) : kMinMatch);
+    info = lz77_parse_segment(words, r0, s0, s1, s1, s1, tables[w], out, mm,
+                              wide_tables ? &W : nullptr,
+                              b.strength > 0 ? b.strength : kSearchStrength);
   }
   if (lane == 0) {
     seg_nseq[w] = info.nseq;

@@ -187,6 +187,46 @@ extern "C"
                                 uint32_t* d_status,
                                 void* cuda_stream);
 
+  /* Encoder autotuner (no reference counterpart): the match finder's search
+   * strength and shortest match are picked per (codec, level, dtype, chunk
+   * shape) by timing candidates on a sample of the first batch's chunks:
+   * among those that compress at most 1 % worse than the defaults, encode
+   * time weighed
+   * against the device-to-host cost of the compressed bytes; the choice is
+   * kept for the process.  Off unless enabled here, by
+   * CHUCKY_AUTOTUNE=1 in the environment, or by a server created with
+   * `autotune` set (chucky_serve.h).  Streams created while it is on tune
+   * at their first batch (the host waits for the trials, tens of ms, once
+   * per key).
+   * chucky_autotune_entries: the table (up to `cap` entries to `out`, which
+   * may be NULL); returns the entry count.
+   * chucky_autotune_pick: the choice among n measured candidates (index),
+   * given encode seconds and compressed bytes for `in_bytes` of input and
+   * the copy-out rate in GB/s: of the candidates whose output is at most
+   * 1 % above `preferred`'s (the smallest output's when `preferred` < 0),
+   * the one of least max(encode, copy-out) + 1/4 min(encode, copy-out); a
+   * candidate within 1 % of that cost loses to `preferred`. */
+  struct chucky_autotune_entry
+  {
+    int codec, level, dtype, rank;
+    uint64_t chunk_shape[16];
+    uint64_t chunk_bytes;
+    int strength;   /* 0: the level's default */
+    int min_match;  /* 0: the level's default */
+    double encode_gbs, ratio; /* of the chosen candidate on the sample */
+    uint32_t candidates;      /* 0: tuning failed, defaults kept */
+  };
+  void chucky_autotune_set_enabled(int on);
+  int chucky_autotune_enabled(void);
+  size_t chucky_autotune_entries(struct chucky_autotune_entry* out, size_t cap);
+  void chucky_autotune_clear(void);
+  int chucky_autotune_pick(const double* enc_s,
+                           const double* out_bytes,
+                           int n,
+                           double in_bytes,
+                           double d2h_gbs,
+                           int preferred);
+
 #ifdef __cplusplus
 }
 #endif

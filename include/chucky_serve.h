@@ -46,6 +46,8 @@ extern "C"
     int batch_encoders;      /* 1: shared encoder engine across streams */
     size_t encoder_wave_bytes; /* engine launch size (0: 256 MiB of input) */
     int encoder_lanes;         /* engine CUDA streams, rounds overlap (0: 2) */
+    int autotune;              /* 1: turn on the encoder autotuner
+                                  (chucky_autotune_set_enabled, process-wide) */
   };
 
   struct chucky_server;
