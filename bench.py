@@ -819,6 +819,18 @@ def autotune_table(lib):
     return {"enabled": bool(lib.chucky_autotune_enabled()), "entries": out}
 
 
+def child_leg(name, args):
+    """One single-stream leg (`--single orca-e2e` / `cube-appends`) run by
+    this script in a child process; its JSON result."""
+    import subprocess
+    r = subprocess.run([sys.executable, os.path.abspath(__file__), "--single", name,
+                        "--steps", str(max(3, args.steps // 2))],
+                       capture_output=True, text=True, timeout=1800)
+    if r.returncode != 0:
+        raise RuntimeError(f"{name} leg failed:\n{r.stderr[-2000:]}")
+    return json.loads(r.stdout.strip().splitlines()[-1])
+
+
 def run_served_bench(args, rank, world):
     import torch
     import chucky_gb300 as cg
@@ -829,6 +841,12 @@ def run_served_bench(args, rank, world):
     lib.chucky_launch_count.restype = C.c_uint64
     dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
     torch.cuda.set_device(dev)
+    # the Orca-shaped and cube legs in a child process, before this one pins
+    # the served form's inputs: in-process after the served legs (4.8 GB of
+    # their inputs still pinned) the same Orca-shaped stream measured 35-40 %
+    # slower
+    orca = child_leg("orca-e2e", args) if rank == 0 else None
+    cube = child_leg("cube-appends", args) if rank == 0 else None
     sink = lib.chucky_discard_sink_create()
     import dataclasses
     host_reqs = serve.c5_requests()                   # pinned host inputs
@@ -867,8 +885,6 @@ def run_served_bench(args, rank, world):
     lib.chucky_discard_sink_destroy(sink)
     del dev_reqs
     torch.cuda.empty_cache()
-    orca = orca_e2e(lib, dev, max(3, args.steps // 2))
-    cube = cube_appends(lib, dev, max(3, args.steps // 2))
     enc = encoder_roofline(lib, dev, "lz4")
     enc_z = encoder_roofline(lib, dev, "zstd")
     ratios = codec_ratios(lib, dev) if rank == 0 else None
@@ -1148,6 +1164,11 @@ def run_single(args):
         slib.chucky_discard_sink_destroy(sink)
         print("ok", flush=True)
         return
+    if args.single in ("orca-e2e", "cube-appends"):
+        lib.tile_stream_gpu_restart.argtypes = [C.c_void_p, C.c_void_p]
+        leg = orca_e2e if args.single == "orca-e2e" else cube_appends
+        print(json.dumps(leg(lib, torch.device("cuda"), args.steps)), flush=True)
+        return
     if args.single in ("encode-lz4", "encode-zstd"):
         # the encoder launch set alone on a batch of sensor chunks (48 chunks
         # of 32 x 256 x 256 u16, 192 MiB: more than L2): the ncu case
@@ -1200,7 +1221,7 @@ def main():
                     help="sensor frames per step (multiple of 32)")
     ap.add_argument("--single", choices=["u16", "f32", "cube-lz4", "sensor-zstd",
                                          "sensor-lz4", "encode-lz4", "encode-zstd",
-                                         "served-pass"],
+                                         "served-pass", "orca-e2e", "cube-appends"],
                     help="profiling case: one array's stream, --steps passes, no timing")
     ap.add_argument("--level", type=int, default=None,
                     help="codec level of --single encode-* (default 1)")

@@ -28,8 +28,8 @@ namespace chucky {
 
 namespace {
 
-// 32 KiB blocks: every block builds its own Huffman table serially, so
-// smaller blocks put more of them in flight (the table costs ~0.3% ratio)
+// 8 KiB blocks: a CTA per block, whose serial parts (the three FSE state
+// chains) grow with the block's sequences
 constexpr uint32_t kBlockLog = 13;
 constexpr uint32_t kBlockBytes = 1u << kBlockLog; // 8 KiB
 constexpr uint32_t kSegsPerBlock = kBlockBytes / kSegBytes;

@@ -4,7 +4,7 @@
 // available, so out-of-bounds and misaligned accesses abort with a report.
 //
 // usage: codec_emu <lz4|zstd> <chunk_bytes> <n_chunks> <pattern> <seed>
-//                  [refs] [level=<n>]
+//                  [refs] [level=<n>] [strength=<n>] [mm=<n>]
 #include "simt.hpp"
 
 #include "../../chucky_gb300/csrc/lz4.cu"
@@ -115,13 +115,17 @@ int main(int argc, char** argv)
   const std::string pat = argv[4];
   rng_state = std::stoull(argv[5]);
   bool refs_mode = false;
-  int level = 1;
+  int level = 1, strength = 0, min_match = 0;
   for (int a = 6; a < argc; ++a) {
     const std::string opt = argv[a];
     if (opt == "refs")
       refs_mode = true;
     else if (opt.rfind("level=", 0) == 0)
       level = std::stoi(opt.substr(6));
+    else if (opt.rfind("strength=", 0) == 0)
+      strength = std::stoi(opt.substr(9));
+    else if (opt.rfind("mm=", 0) == 0)
+      min_match = std::stoi(opt.substr(3));
   }
   const uint64_t in_stride = (chunk + 255) / 256 * 256;
   const uint64_t bound = codec == "zstd"
@@ -143,6 +147,8 @@ int main(int argc, char** argv)
   b.out_stride = out_stride;
   b.out_sizes = sizes.data();
   b.level = level;
+  b.strength = strength;
+  b.min_match = min_match;
   const size_t sb = codec == "zstd" ? zstd_scratch_bytes(n, chunk, level)
                                     : lz4_scratch_bytes(n, chunk, level);
   std::vector<uint8_t> scratch(sb);
@@ -336,6 +342,8 @@ int main(int argc, char** argv)
     rb.chunk_bytes = chunk;
     rb.n_chunks = n;
     rb.level = level;
+    rb.strength = strength;
+    rb.min_match = min_match;
     rb.refs = refs.data();
     std::vector<uint8_t> scratch2(sb, 0x5A);
     if ((codec == "zstd" ? launch_zstd(rb, scratch2.data(), nullptr)
