@@ -982,8 +982,13 @@ int Stream::deliver(int si)
     if (!D.d_data)
       continue;
     const uint64_t total = D.offsets[D.positions];
-    // (bytes beyond the expected size arrived by the tail kernel)
-    agg_estimate[l] = total + total / 32 + (16u << 10);
+    // (bytes beyond the expected size arrived by the tail kernel).  The
+    // larger of the last two batches: a partial batch (a request's last)
+    // does not shrink the copy of the full one after it (the next request
+    // on this stream)
+    const uint64_t base = std::max(total, agg_prev_total[l]);
+    agg_prev_total[l] = total;
+    agg_estimate[l] = base + base / 32 + (16u << 10);
   }
   const double t0 = now_ms();
   uint64_t bytes_out = 0;

@@ -158,6 +158,7 @@ struct Stream
   // bytes per level copied device -> host with the batch (the rest, if
   // any, at delivery): the last batch's size plus a margin
   uint64_t agg_estimate[LOD_MAX_LEVELS] = {};
+  uint64_t agg_prev_total[LOD_MAX_LEVELS] = {}; // the batch before the last
   uint64_t agg_scratch_slot = 0; // entries per delivery slot
   DeliverySlot slot[2];
   cudaEvent_t ev_batch[2] = {};
