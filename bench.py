@@ -861,7 +861,8 @@ def run_served_bench(args, rank, world):
     clocks = Clocks()
     # the served form: one server (start-up: a resident stream per request),
     # device-input passes, host-input passes, then the paced latency pass
-    with serve.Server(48 << 30, 16, True, autotune=args.autotune) as srv:
+    with serve.Server(48 << 30, 16, True, autotune=args.autotune,
+                      batch_deadline_ms=args.batch_deadline_ms) as srv:
         srv.prewarm(host_reqs, sink, per_request=True)
         if rank == 0:
             clocks.start()
@@ -875,7 +876,8 @@ def run_served_bench(args, rank, world):
         lat_ms = _server_pass(srv, host_reqs, sink, paced=True)
         lat = srv.stats()
     # the plain form: one request at a time, each stream encoding on its own
-    with serve.Server(1 << 62, 1, False, autotune=args.autotune) as psrv:
+    with serve.Server(1 << 62, 1, False, autotune=args.autotune,
+                      batch_deadline_ms=args.batch_deadline_ms) as psrv:
         psrv.prewarm(host_reqs, sink, per_request=False)
         pms_dev, _, _ = timed_passes(psrv, dev_reqs, lib, sink, args.steps, args.warmup)
         pms_host, _, _ = timed_passes(psrv, host_reqs, lib, sink, args.steps,
@@ -913,9 +915,11 @@ def run_served_bench(args, rank, world):
                    "l2": "inputs larger than L2 (4.8 GB per step)",
                    "parallelism": f"replicas x{world}",
                    "served": "chucky_server, 48 GB budget, up to 16 requests open, "
-                             "encoders batched across streams, all requests queued",
+                             "encoders batched across streams, all requests queued, "
+                             "encoder autotuner %s, batch deadline %g ms"
+                             % ("on" if args.autotune else "off", args.batch_deadline_ms),
                    "plain": "the same requests one at a time, each stream encoding on "
-                            "its own"},
+                            "its own (same autotuner and batch deadline)"},
         "e2e": {"value": round(e2e, 3), "unit": "GB/s",
                 "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": int(out_h),
                 "ms_per_step": round(totals[1] / args.steps, 3),
@@ -1156,7 +1160,8 @@ def run_single(args):
                 on_dev[id(r.data)] = r.data.to(dev)
         reqs = [dataclasses.replace(r, data=on_dev[id(r.data)], _cfg=None) for r in host]
         sink = slib.chucky_discard_sink_create()
-        with serve.Server(48 << 30, 16, True, autotune=args.autotune) as srv:
+        with serve.Server(48 << 30, 16, True, autotune=args.autotune,
+                          batch_deadline_ms=args.batch_deadline_ms) as srv:
             srv.prewarm(reqs, sink, per_request=True)
             for _ in range(1 + args.steps):
                 srv.replay(reqs, sink, paced=False)
@@ -1225,6 +1230,9 @@ def main():
                     help="profiling case: one array's stream, --steps passes, no timing")
     ap.add_argument("--level", type=int, default=None,
                     help="codec level of --single encode-* (default 1)")
+    ap.add_argument("--batch-deadline-ms", type=float, default=10.0,
+                    help="served and plain forms: a stream starts a partial batch once "
+                         "its oldest epoch has waited this long (0: full batches only)")
     ap.add_argument("--autotune", type=int, default=1, choices=[0, 1],
                     help="served form: encoder autotuner on (1, default) or off (0); "
                          "the plain form of the same run uses the same choice")

@@ -206,7 +206,8 @@ def bind_zarr_fs_sink(lib):
 class ServerConfig(C.Structure):
     _fields_ = [("hbm_budget_bytes", C.c_size_t), ("max_streams", C.c_int),
                 ("batch_encoders", C.c_int), ("encoder_wave_bytes", C.c_size_t),
-                ("encoder_lanes", C.c_int), ("autotune", C.c_int)]
+                ("encoder_lanes", C.c_int), ("autotune", C.c_int),
+                ("batch_deadline_ms", C.c_double)]
 
 
 class AutotuneEntry(C.Structure):

@@ -108,7 +108,8 @@ struct chucky_request
 extern "C" chucky_server*
 chucky_server_create(const chucky_server_config* config)
 {
-  if (!config || config->max_streams < 1 || !config->hbm_budget_bytes)
+  if (!config || config->max_streams < 1 || !config->hbm_budget_bytes ||
+      !(config->batch_deadline_ms >= 0))
     return nullptr;
   auto* s = new (std::nothrow) chucky_server();
   if (!s)
@@ -190,6 +191,7 @@ chucky_server_open(chucky_server* s,
         s->peak_open = std::max<uint64_t>(s->peak_open, s->open);
         lk.unlock();
         if (tile_stream_gpu_restart(got.s, sink) == 0) {
+          tile_stream_gpu_set_batch_deadline(got.s, s->cfg.batch_deadline_ms);
           auto* r = new chucky_request{ s, got.s, got.bytes, key };
           return r;
         }
@@ -228,6 +230,7 @@ chucky_server_open(chucky_server* s,
           s->cv.notify_all();
           return nullptr;
         }
+        tile_stream_gpu_set_batch_deadline(st, s->cfg.batch_deadline_ms);
         return new chucky_request{ s, st, need, key };
       }
       if (!victims.empty()) {

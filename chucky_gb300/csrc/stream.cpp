@@ -1120,6 +1120,28 @@ int Stream::drain_all()
   return 0;
 }
 
+int Stream::deliver_ready()
+{
+  for (int k = 0; k < 2; ++k) {
+    int first = -1;
+    for (int i = 0; i < 2; ++i)
+      if (slot[i].busy && (first < 0 || slot[i].seq < slot[first].seq))
+        first = i;
+    if (first < 0)
+      return 0;
+    const cudaError_t q = cudaEventQuery(ev_batch[first]);
+    if (q == cudaErrorNotReady)
+      return 0;
+    if (q != cudaSuccess) {
+      std::fprintf(stderr, "chucky_gb300: batch failed: %s\n", cudaGetErrorString(q));
+      return 1;
+    }
+    if (deliver(first))
+      return 1;
+  }
+  return 0;
+}
+
 int Stream::batch_boundary()
 {
   // The previous batch is delivered while this one runs on the GPU: now if
@@ -1266,6 +1288,16 @@ writer_result Stream::append_async(slice in, cudaStream_t producer)
       if (accumulated == P.K && batch_boundary())
         return writer_error_at(src, end);
     }
+  }
+  if (batch_deadline_ms > 0) {
+    // latency bound: the batch being filled goes as a partial batch once
+    // its oldest epoch has waited the deadline, and finished batches are
+    // delivered now rather than at the next kick
+    if (accumulated > 0 && !pending_epoch_ms.empty() &&
+        now_ms() - pending_epoch_ms.front() >= batch_deadline_ms && batch_boundary())
+      return writer_error_at(src, end);
+    if (deliver_ready())
+      return writer_error_at(src, end);
   }
   if (producer) {
     // the producer's later work (e.g. overwriting its buffer) waits for
@@ -1587,4 +1619,13 @@ extern "C" void
 tile_stream_gpu_clear_latencies(tile_stream_gpu* s)
 {
   s->impl.latencies_ms.clear();
+}
+
+extern "C" int
+tile_stream_gpu_set_batch_deadline(tile_stream_gpu* s, double ms)
+{
+  if (!s || !(ms >= 0))
+    return 1;
+  s->impl.batch_deadline_ms = ms;
+  return 0;
 }

@@ -178,6 +178,9 @@ struct Stream
 
   // append-to-delivered latency per epoch (ms)
   std::vector<double> pending_epoch_ms; // epochs of the batch being filled
+  // > 0: an append starts the batch being filled as a partial batch once
+  // its oldest epoch has waited this long, and delivers finished batches
+  double batch_deadline_ms = 0;
   std::vector<double> latencies_ms;
 
   // progress
@@ -215,6 +218,7 @@ struct Stream
   int batch_boundary();
   int deliver(int si);
   int drain_all();
+  int deliver_ready(); // deliver the batches the GPU has finished, in order
   int finalize_level(int l);
   int write_index_blobs(int l, const uint8_t* blobs);
   cudaStream_t agg_stream() const { return cfg.codec.id != CODEC_NONE ? s_agg : s_comp; }

@@ -70,10 +70,11 @@ class Server:
     """Owner of one chucky_server."""
 
     def __init__(self, hbm_budget=48 << 30, max_streams=16, batch_encoders=True,
-                 wave_bytes=0, lanes=0, autotune=False):
+                 wave_bytes=0, lanes=0, autotune=False, batch_deadline_ms=0.0):
         self.lib = _lib()
         cfg = capi.ServerConfig(hbm_budget, max_streams, 1 if batch_encoders else 0,
-                                wave_bytes, lanes, 1 if autotune else 0)
+                                wave_bytes, lanes, 1 if autotune else 0,
+                                float(batch_deadline_ms))
         self.h = self.lib.chucky_server_create(C.byref(cfg))
         if not self.h:
             raise RuntimeError("chucky_server_create failed")

@@ -48,6 +48,18 @@ extern "C"
                                    size_t cap);
   void tile_stream_gpu_clear_latencies(struct tile_stream_gpu* s);
 
+  /* Latency bound for streams fed in small appends (no reference
+   * counterpart: the reference delivers a batch when its K epochs are in,
+   * src/stream/config.c:31-45).  With `ms` > 0, an append that finds the
+   * oldest finished epoch of the batch being filled older than `ms`
+   * starts that batch with the epochs it has (a partial batch, as a flush
+   * does), and every append delivers the batches the GPU has finished
+   * instead of leaving them to the next batch.  The shard bytes do not
+   * change (chunks and their order within shards are the same) except
+   * where the shard alignment pads each batch's group of chunks.  0 (the
+   * default) turns it off.  Returns 0, or 1 for a negative `ms`. */
+  int tile_stream_gpu_set_batch_deadline(struct tile_stream_gpu* s, double ms);
+
   /* A shard sink that discards every byte and counts them (the metering
    * sink of a throughput benchmark). */
   struct shard_sink* chucky_discard_sink_create(void);

@@ -48,6 +48,10 @@ extern "C"
     int encoder_lanes;         /* engine CUDA streams, rounds overlap (0: 2) */
     int autotune;              /* 1: turn on the encoder autotuner
                                   (chucky_autotune_set_enabled, process-wide) */
+    double batch_deadline_ms;  /* > 0: every request's stream starts a
+                                  partial batch once its oldest epoch has
+                                  waited this long
+                                  (tile_stream_gpu_set_batch_deadline) */
   };
 
   struct chucky_server;

@@ -185,12 +185,17 @@ def parse_shard(blob, n_slots, alignment=0):
     return index, ok
 
 
-def run_gpu(cfg, data, pieces=None):
-    """This library's GPU stream on the same input (needs a GPU)."""
+def run_gpu(cfg, data, pieces=None, deadline_ms=None):
+    """This library's GPU stream on the same input (needs a GPU); with
+    `deadline_ms`, the stream's batch deadline (partial batches)."""
     import chucky_gb300 as cg
     sink = MemSink()
     try:
         s = cg.GpuStream(cfg, sink.base)
+        if deadline_ms is not None:
+            s.lib.tile_stream_gpu_set_batch_deadline.argtypes = [C.c_void_p, C.c_double]
+            if s.lib.tile_stream_gpu_set_batch_deadline(s.h, float(deadline_ms)) != 0:
+                raise RuntimeError("tile_stream_gpu_set_batch_deadline failed")
         try:
             _drive(s.writer, data, pieces)
             cursor = s.cursor()
