@@ -109,6 +109,16 @@ __device__ __forceinline__ uint32_t hash4w(uint32_t v, int hlog)
   return (v * 2654435761u) >> (32 - hlog);
 }
 
+// Table entries: the region offset (14 bits) and, in the two spare bits, a
+// tag -- the two hash bits below the table's -- so that most entries of
+// other values are passed over without loading their bytes; 0xFFFF: none
+// (offsets are at most kRegionBytes - 4).
+static_assert(kRegionLog == 14, "region offsets fill 14 bits of an entry");
+__device__ __forceinline__ uint32_t wide_tag(uint32_t v, int hlog)
+{
+  return ((v * 2654435761u) >> (30 - hlog)) & 3u;
+}
+
 // 4 bytes of `base` (4-byte aligned) at any byte position p
 __device__ __forceinline__ uint32_t load4(const uint8_t* base, uint32_t p)
 {
@@ -184,33 +194,39 @@ __device__ __forceinline__ uint32_t lane_match(const uint32_t* words,
 
 // Candidates of a position q (region-relative, 4 bytes x) in the wide
 // window's earlier regions, nearest region first; the first that matches
-// longer than (cand, len) replaces them and ends the search.  The bytes
-// at q come from the staged region `words`, the candidate's from the chunk
-// in global memory.
+// longer than (cand, len) replaces them and ends the search.  Only entries
+// with the value's tag are checked against the chunk (its bytes in global
+// memory, the lane's from the staged region `words`).
 __device__ __forceinline__ void wide_probe(const WideWindow& W,
                                            const uint32_t* words,
                                            uint32_t r0,
                                            uint32_t q,
                                            uint32_t x,
                                            uint32_t end,
+                                           uint32_t step,
                                            bool& ok,
                                            uint32_t& cand,
                                            uint32_t& len)
 {
   const uint32_t qa = r0 + q; // chunk position
   const uint32_t h = hash4w(x, W.hlog);
+  const uint32_t tag = wide_tag(x, W.hlog);
+  const uint64_t entries = wide_entries(W.hlog);
+  // where probing has thinned out (a literal run: the data is locally
+  // incompressible) only the two nearest regions
+  const uint32_t nb = min(step > 1 ? min(W.back, 2u) : W.back, W.region);
   const uint32_t cap = min(kLaneExtend - 1, end - q);
   const uint32_t need = ok ? len + 1 : 4;
-  for (uint32_t k = 1; k <= W.back && k <= W.region; ++k) {
-    const uint32_t rr = W.region - k;
-    const uint16_t t = W.tables[uint64_t(rr) * wide_entries(W.hlog) + h];
-    if (t == 0xFFFF)
-      continue;
-    const uint32_t c = rr * kRegionBytes + t;
+  for (uint32_t k = 0; k < nb; ++k) {
+    const uint32_t rr = W.region - 1 - k;
+    const uint16_t t = W.tables[uint64_t(rr) * entries + h];
+    if (t == 0xFFFF || (uint32_t(t) >> 14) != tag)
+      continue; // none, or another value (its tag differs)
+    const uint32_t c = rr * kRegionBytes + (t & 0x3FFFu);
     if (qa - c > W.max_dist)
       break; // the regions further back are further still
     if (load4(W.chunk, c) != x)
-      continue; // another value with the same hash
+      continue; // another value with the same hash and tag
     uint32_t m = 4;
     while (m + 4 <= cap) {
       const uint32_t d = word_at(words, q + m) ^ load4(W.chunk, c + m);
@@ -407,9 +423,9 @@ __device__ inline SegInfo lz77_parse_segment(const uint32_t* words,
     uint32_t lb = okb ? lane_match(words, bytes, qb, cb, end) : 0;
     if (wide) { // earlier regions, for lanes without a good local match
       if (va && la < kWideProbeBelow)
-        wide_probe(*wide, words, r0, qa, xa, end, oka, ca, la);
+        wide_probe(*wide, words, r0, qa, xa, end, step, oka, ca, la);
       if (vb && lb < kWideProbeBelow)
-        wide_probe(*wide, words, r0, qb, xb, end, okb, cb, lb);
+        wide_probe(*wide, words, r0, qb, xb, end, step, okb, cb, lb);
     }
     __syncwarp();
     if (va)
@@ -550,7 +566,7 @@ __device__ inline uint32_t lz77_compact_literals(uint32_t* words,
 
 // The wide window's first pass: one CTA per region, the last position of
 // every hash of 4 bytes within the region (a maximum: the same table in
-// any thread order), written as 16-bit region offsets (0xFFFF: none).
+// any thread order), written as 16-bit entries (offset and tag, above).
 // `in_at(c)` gives chunk c's bytes; `rpc` regions per chunk.  The region is
 // staged and the table built in dynamic shared memory
 // (wide_index_smem(hlog) bytes).
@@ -577,16 +593,20 @@ lz77_index_k(Batch b, uint16_t* tables, uint32_t rpc, int hlog)
   for (uint32_t i = threadIdx.x; i < entries / 4; i += blockDim.x)
     t4[i] = make_uint4(0, 0, 0, 0);
   lz77_stage_region(base, r0, r1, words, threadIdx.x, blockDim.x); // (ends with a barrier)
-  // positions whose 4 bytes lie in the region
-  for (uint32_t p = threadIdx.x; p + 4 <= r1 - r0; p += blockDim.x)
-    atomicMax(&tbl[hash4w(word_at(words, p), hlog)], p + 1);
+  // positions whose 4 bytes lie in the region: (offset + 1) << 2 | tag,
+  // so the maximum is the last position
+  for (uint32_t p = threadIdx.x; p + 4 <= r1 - r0; p += blockDim.x) {
+    const uint32_t v = word_at(words, p);
+    atomicMax(&tbl[hash4w(v, hlog)], ((p + 1) << 2) | wide_tag(v, hlog));
+  }
   __syncthreads();
   // two entries per thread and step: 4-byte stores
+  auto entry = [](uint32_t a) {
+    return a ? ((a & 3u) << 14) | ((a >> 2) - 1) : 0xFFFFu;
+  };
   uint32_t* out = reinterpret_cast<uint32_t*>(tables + (chunk * rpc + region) * entries);
-  for (uint32_t i = threadIdx.x; i < entries / 2; i += blockDim.x) {
-    const uint32_t a = tbl[2 * i], c = tbl[2 * i + 1];
-    out[i] = (a ? a - 1 : 0xFFFFu) | ((c ? c - 1 : 0xFFFFu) << 16);
-  }
+  for (uint32_t i = threadIdx.x; i < entries / 2; i += blockDim.x)
+    out[i] = entry(tbl[2 * i]) | (entry(tbl[2 * i + 1]) << 16);
 }
 
 // Launches lz77_index_k over every region of a batch (`tables`: 4-byte
