@@ -192,62 +192,119 @@ __device__ __forceinline__ uint32_t lane_match(const uint32_t* words,
   return len;
 }
 
-// Candidates of a position q (region-relative, 4 bytes x) in the wide
-// window's earlier regions, nearest region first; the first that matches
-// longer than (cand, len) replaces them and ends the search.  Only entries
-// with the value's tag are checked against the chunk (its bytes in global
-// memory, the lane's from the staged region `words`).
-__device__ __forceinline__ void wide_probe(const WideWindow& W,
-                                           const uint32_t* words,
-                                           uint32_t r0,
-                                           uint32_t q,
-                                           uint32_t x,
-                                           uint32_t end,
-                                           uint32_t step,
-                                           bool& ok,
-                                           uint32_t& cand,
-                                           uint32_t& len)
+// Match length of candidate c (chunk position) for position q (region
+// position, its bytes in the staged region) whose first 4 bytes are known
+// equal, up to `cap` bytes.
+__device__ __forceinline__ uint32_t wide_extend(const WideWindow& W,
+                                                const uint32_t* words,
+                                                uint32_t q,
+                                                uint32_t c,
+                                                uint32_t cap)
 {
-  const uint32_t qa = r0 + q; // chunk position
-  const uint32_t h = hash4w(x, W.hlog);
-  const uint32_t tag = wide_tag(x, W.hlog);
+  uint32_t m = 4;
+  while (m + 4 <= cap) {
+    const uint32_t d = word_at(words, q + m) ^ load4(W.chunk, c + m);
+    if (d) {
+      m += uint32_t(__ffs(int(d)) - 1) >> 3;
+      break;
+    }
+    m += 4;
+  }
+  if (m + 4 > cap) { // the last bytes before the cap, one by one
+    const uint8_t* bytes = reinterpret_cast<const uint8_t*>(words);
+    while (m < cap && bytes[q + m] == W.chunk[c + m])
+      ++m;
+  }
+  return m > cap ? cap : m;
+}
+
+// One lane's probe of the wide window for one position.
+struct WideLane
+{
+  bool on;        // still searching
+  uint32_t q, x;  // position (region-relative) and its 4 bytes
+  uint32_t h, tag;
+  uint32_t cap, need;
+};
+
+__device__ __forceinline__ WideLane wide_lane(const WideWindow& W,
+                                              bool probe,
+                                              uint32_t q,
+                                              uint32_t x,
+                                              uint32_t end,
+                                              bool ok,
+                                              uint32_t len)
+{
+  WideLane L;
+  L.on = probe;
+  L.q = q;
+  L.x = x;
+  L.h = hash4w(x, W.hlog);
+  L.tag = wide_tag(x, W.hlog);
+  L.cap = probe ? min(kLaneExtend - 1, end - q) : 0;
+  L.need = ok ? len + 1 : 4;
+  return L;
+}
+
+// Candidates of two positions of a lane (its a and b windows) in the wide
+// window's earlier regions, nearest region first; for each, the first
+// candidate that matches longer than its (cand, len) replaces them and
+// ends its search.  Only entries with the value's tag are checked against
+// the chunk (its bytes in global memory, the lane's from the staged region
+// `words`).  The two searches are independent; their loads are issued side
+// by side.  Where probing has thinned out (`step` > 1: a literal run) only
+// the two nearest regions are probed.
+__device__ __forceinline__ void wide_probe2(const WideWindow& W,
+                                            const uint32_t* words,
+                                            uint32_t r0,
+                                            uint32_t step,
+                                            WideLane A,
+                                            bool& oka,
+                                            uint32_t& ca,
+                                            uint32_t& la,
+                                            WideLane B,
+                                            bool& okb,
+                                            uint32_t& cb,
+                                            uint32_t& lb)
+{
   const uint64_t entries = wide_entries(W.hlog);
-  // where probing has thinned out (a literal run: the data is locally
-  // incompressible) only the two nearest regions
   const uint32_t nb = min(step > 1 ? min(W.back, 2u) : W.back, W.region);
-  const uint32_t cap = min(kLaneExtend - 1, end - q);
-  const uint32_t need = ok ? len + 1 : 4;
-  for (uint32_t k = 0; k < nb; ++k) {
+  for (uint32_t k = 0; k < nb && (A.on || B.on); ++k) {
     const uint32_t rr = W.region - 1 - k;
-    const uint16_t t = W.tables[uint64_t(rr) * entries + h];
-    if (t == 0xFFFF || (uint32_t(t) >> 14) != tag)
-      continue; // none, or another value (its tag differs)
-    const uint32_t c = rr * kRegionBytes + (t & 0x3FFFu);
-    if (qa - c > W.max_dist)
-      break; // the regions further back are further still
-    if (load4(W.chunk, c) != x)
-      continue; // another value with the same hash and tag
-    uint32_t m = 4;
-    while (m + 4 <= cap) {
-      const uint32_t d = word_at(words, q + m) ^ load4(W.chunk, c + m);
-      if (d) {
-        m += uint32_t(__ffs(int(d)) - 1) >> 3;
-        break;
+    const uint16_t* tb = W.tables + uint64_t(rr) * entries;
+    const uint16_t ta = A.on ? tb[A.h] : uint16_t(0xFFFF);
+    const uint16_t tbb = B.on ? tb[B.h] : uint16_t(0xFFFF);
+    const bool ga = ta != 0xFFFF && (uint32_t(ta) >> 14) == A.tag;
+    const bool gb = tbb != 0xFFFF && (uint32_t(tbb) >> 14) == B.tag;
+    const uint32_t cxa = rr * kRegionBytes + (ta & 0x3FFFu);
+    const uint32_t cxb = rr * kRegionBytes + (tbb & 0x3FFFu);
+    // the regions further back are further still
+    const bool fa = ga && r0 + A.q - cxa > W.max_dist;
+    const bool fb = gb && r0 + B.q - cxb > W.max_dist;
+    if (fa)
+      A.on = false;
+    if (fb)
+      B.on = false;
+    const bool va = ga && !fa, vb = gb && !fb;
+    const uint32_t xa = va ? load4(W.chunk, cxa) : ~A.x;
+    const uint32_t xb = vb ? load4(W.chunk, cxb) : ~B.x;
+    if (va && xa == A.x) {
+      const uint32_t m = wide_extend(W, words, A.q, cxa, A.cap);
+      if (m >= A.need) {
+        oka = true;
+        la = m;
+        ca = cxa - r0; // before the region: wraps, offsets stay q - cand
+        A.on = false;
       }
-      m += 4;
     }
-    if (m + 4 > cap) { // the last bytes before the cap, one by one
-      const uint8_t* bytes = reinterpret_cast<const uint8_t*>(words);
-      while (m < cap && bytes[q + m] == W.chunk[c + m])
-        ++m;
-    }
-    if (m > cap)
-      m = cap;
-    if (m >= need) {
-      ok = true;
-      len = m;
-      cand = c - r0; // before the region: wraps, offsets stay q - cand
-      return;
+    if (vb && xb == B.x) {
+      const uint32_t m = wide_extend(W, words, B.q, cxb, B.cap);
+      if (m >= B.need) {
+        okb = true;
+        lb = m;
+        cb = cxb - r0;
+        B.on = false;
+      }
     }
   }
 }
@@ -422,10 +479,10 @@ __device__ inline SegInfo lz77_parse_segment(const uint32_t* words,
     uint32_t la = oka ? lane_match(words, bytes, qa, ca, end) : 0;
     uint32_t lb = okb ? lane_match(words, bytes, qb, cb, end) : 0;
     if (wide) { // earlier regions, for lanes without a good local match
-      if (va && la < kWideProbeBelow)
-        wide_probe(*wide, words, r0, qa, xa, end, step, oka, ca, la);
-      if (vb && lb < kWideProbeBelow)
-        wide_probe(*wide, words, r0, qb, xb, end, step, okb, cb, lb);
+      const bool pa = va && la < kWideProbeBelow, pb = vb && lb < kWideProbeBelow;
+      if (pa || pb)
+        wide_probe2(*wide, words, r0, step, wide_lane(*wide, pa, qa, xa, end, oka, la), oka,
+                    ca, la, wide_lane(*wide, pb, qb, xb, end, okb, lb), okb, cb, lb);
     }
     __syncwarp();
     if (va)
