@@ -132,13 +132,14 @@ class Server:
 
 
 def run_form(requests, hbm_budget, max_streams, batch_encoders, paced, sink=None,
-             warmup=True):
+             warmup=True, batch_deadline_ms=0.0):
     """Warm-up pass (creates the resident streams), then the timed pass."""
     lib = _lib()
     own = sink is None
     sink = sink or lib.chucky_discard_sink_create()
     try:
-        with Server(hbm_budget, max_streams, batch_encoders) as srv:
+        with Server(hbm_budget, max_streams, batch_encoders,
+                    batch_deadline_ms=batch_deadline_ms) as srv:
             srv.prewarm(requests, sink, per_request=max_streams > 1)
             if warmup:
                 srv.replay(requests, sink, paced=False)
@@ -160,9 +161,9 @@ def run_plain(requests, sink=None, warmup=True):
 
 
 def run_served(requests, hbm_budget=48 << 30, max_streams=16, batch_encoders=True,
-               paced=True, sink=None, warmup=True):
+               paced=True, sink=None, warmup=True, batch_deadline_ms=0.0):
     return run_form(requests, hbm_budget, max_streams, batch_encoders, paced, sink=sink,
-                    warmup=warmup)
+                    warmup=warmup, batch_deadline_ms=batch_deadline_ms)
 
 
 def memory_estimate(req):

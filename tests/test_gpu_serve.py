@@ -31,7 +31,10 @@ def _requests(sinks):
     return reqs
 
 
-def test_served_matches_alone():
+@pytest.mark.parametrize("deadline_ms", [0.0, 2.0])
+def test_served_matches_alone(deadline_ms):
+    """With a batch deadline the mixed pass also starts partial batches
+    (paced appends) and delivers finished ones at each append."""
     from chucky_gb300 import serve
     n = 8
     alone_sinks = [MemSink() for _ in range(n)]
@@ -45,7 +48,7 @@ def test_served_matches_alone():
         # restarted (reused) streams both happen
         budget = 3 * max(serve.memory_estimate(r) for r in reqs)
         st = serve.run_served(reqs, hbm_budget=budget, max_streams=4, paced=True,
-                              warmup=False)
+                              warmup=False, batch_deadline_ms=deadline_ms)
         assert st["requests"] == n and st["epochs"] > 0
         assert st["engine_rounds"] > 0 and st["engine_jobs"] >= st["engine_rounds"]
         assert st["streams_reused"] + st["streams_created"] == n
