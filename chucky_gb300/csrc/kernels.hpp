@@ -96,6 +96,7 @@ struct LodTileArgs
     const uint64_t* chunk_fixed;   // [fixed] slot offset per slice
     uint64_t accum_off;            // level start in the accumulators
     uint64_t nelem;                // product of shape
+    uint32_t off32;                // offsets within a chunk fit 32 bits
   } lv[16];
 };
 int lod_tile_levels(int lod_ndim);

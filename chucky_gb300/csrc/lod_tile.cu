@@ -266,6 +266,19 @@ lod_tile_k(LodTileArgs a)
     const bool fold = (a.fold_mask >> l) & 1;
     const bool emit = (a.emit_mask >> l) & 1;
     const uint64_t fixedl = a.lv[l].chunk_fixed ? a.lv[l].chunk_fixed[b] : 0;
+    // 32-bit index arithmetic where it fits: offsets within the parent
+    // tile's chunk, and a slice's accumulator index (the slice's base
+    // pointer once per level)
+    uint32_t s32[3], shp32[3];
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+      s32[k] = uint32_t(a.lv[l].s[k]);
+      shp32[k] = uint32_t(a.lv[l].shape[k]);
+    }
+    const bool ai32 = a.lv[l].nelem <= 0xFFFFFFFFull;
+    T* const accb = fold ? reinterpret_cast<T*>(a.accum) + a.lv[l].accum_off +
+                             b * a.lv[l].nelem
+                         : nullptr;
     // the parent tile lies inside one chunk along every dim: chunk offsets
     // are a tile base plus within-chunk strides (no per-element division)
     bool inchunk = true;
@@ -276,6 +289,7 @@ lod_tile_k(LodTileArgs a)
       tbase += uint64_t(porg[k] / a.cs[k]) * a.lv[l].S[k] +
                uint64_t(porg[k] % a.cs[k]) * a.lv[l].s[k];
     }
+    const bool off32 = inchunk && a.lv[l].off32;
     for (int i = threadIdx.x; i < pn; i += kTileThreads) {
       uint32_t p[3], in = 1;
       int r = i;
@@ -329,23 +343,41 @@ lod_tile_k(LodTileArgs a)
         pi = (pi << plog) + int(p[k]);
       nxt[pi] = v;
       uint32_t gx[3];
-      uint64_t pos = tbase;
 #pragma unroll
-      for (int k = 0; k < D; ++k) {
+      for (int k = 0; k < D; ++k)
         gx[k] = porg[k] + p[k];
-        pos += uint64_t(p[k]) * a.lv[l].s[k];
-      }
-      if (!inchunk)
+      uint64_t pos;
+      if (off32) {
+        uint32_t o = 0;
+#pragma unroll
+        for (int k = 0; k < D; ++k)
+          o += p[k] * s32[k];
+        pos = tbase + o;
+      } else if (inchunk) {
+        pos = tbase;
+#pragma unroll
+        for (int k = 0; k < D; ++k)
+          pos += uint64_t(p[k]) * a.lv[l].s[k];
+      } else {
         pos = fixedl + chunk_pos<D>(a, l, gx);
+      }
       if (fold) {
         // dense accumulator [fixed][row-major level coords]; its value
         // before this epoch is in the stage
-        uint64_t ai = 0;
+        T* acc;
+        if (ai32) {
+          uint32_t ai = 0;
 #pragma unroll
-        for (int k = 0; k < D; ++k)
-          ai = ai * a.lv[l].shape[k] + gx[k];
-        T* acc = reinterpret_cast<T*>(a.accum) + a.lv[l].accum_off +
-                 b * a.lv[l].nelem + ai;
+          for (int k = 0; k < D; ++k)
+            ai = ai * shp32[k] + gx[k];
+          acc = accb + ai;
+        } else {
+          uint64_t ai = 0;
+#pragma unroll
+          for (int k = 0; k < D; ++k)
+            ai = ai * a.lv[l].shape[k] + gx[k];
+          acc = accb + ai;
+        }
         const uint32_t cnt = a.count[l];
         const T av =
           cnt == 0 ? v : fold_one<T>(stage[sbase + i], v, l, a.append_method);

@@ -369,6 +369,7 @@ int Stream::setup_lod()
       V.nelem = P.lv[l].lod_nelem;
       V.accum_off = accum_beg[l];
       V.chunk_fixed = d_chunk_fixed[l];
+      V.off32 = uint64_t(L.chunk_stride) <= 0xFFFFFFFFull ? 1u : 0u;
       for (int k = 0; k < P.lod_ndim; ++k) {
         const int d = P.lod_to_dim[k];
         V.shape[k] = P.lv[l].shape[d];
