@@ -57,6 +57,13 @@ WIDE = [("lz4", "xor16", 40000, 1, 2), ("lz4", "mixed", 65536, 2, 2),
 WIDE_SMALL = [(1024, 6), (37, 3), (1, 2)]
 REFS = [("zstd", "mixed", 70000, 3), ("lz4", "mixed", 70000, 3),
         ("zstd", "xor16", 1024, 5), ("lz4", "random", 37, 4)]
+# the autotuner's parse parameters: search strength and shortest match
+TUNED = [("zstd", "mixed", 65536, 2, "strength=4", "mm=12"),
+         ("zstd", "geom", 20000, 1, "strength=8", "mm=6"),
+         ("zstd", "xor16", 40000, 1, "strength=5", "mm=6"),
+         ("lz4", "xor16", 40000, 1, "strength=8", "mm=6"),
+         ("lz4", "random", 70000, 1, "strength=4", "mm=5"),
+         ("lz4", "halves", 70000, 2, "strength=7", "mm=5")]
 
 
 def _key(codec, pattern, chunk, n, *extra):
@@ -74,6 +81,7 @@ def _cases():
              for p in ("zeros", "mixed", "xor16") for ch, n in WIDE_SMALL]
     keys += [_key(c, p, ch, n, "refs", lv) for c, p, ch, n in REFS
              for lv in ("level=1", "level=3")]
+    keys += [_key(c, p, ch, n, st, mm) for c, p, ch, n, st, mm in TUNED]
     return keys
 
 
@@ -126,3 +134,10 @@ def test_encoder_per_chunk_references(runs, codec, pattern, chunk, n, level):
     """Chunks addressed through a per-chunk reference list (the shared
     encoder engine's batches) decode to their bytes."""
     _run(runs, codec, pattern, chunk, n, "refs", level)
+
+
+@pytest.mark.parametrize("codec,pattern,chunk,n,strength,mm", TUNED)
+def test_tuned_parse_parameters(runs, codec, pattern, chunk, n, strength, mm):
+    """Chunks parsed with other search strengths and shortest matches (the
+    autotuner's candidates) decode to their bytes."""
+    _run(runs, codec, pattern, chunk, n, strength, mm)
