@@ -421,56 +421,85 @@ struct Huff
 // Normalize a histogram of weights to 2^al, every present symbol >= 1 and
 // no symbol above half the table (so every state reads >= 1 bit and the
 // decoder's end-of-stream test fires exactly after the last weight).
-__device__ void norm_weights(const uint32_t* hist, int nsym, int al, int16_t* norm)
+__device__ void norm_weights(const uint32_t* hist_s, int nsym, int al, int16_t* norm_s)
 {
+  // nsym <= 16: counts and the result live in registers (every index below
+  // is a compile-time constant after unrolling), so the serial loops do not
+  // wait on shared memory
   const int size = 1 << al, half = size / 2;
+  uint32_t hist[16];
+  int norm[16];
   uint32_t total = 0;
   int present = 0;
-  for (int s = 0; s < nsym; ++s) {
+#pragma unroll
+  for (int s = 0; s < 16; ++s) {
+    hist[s] = s < nsym ? hist_s[s] : 0u;
     total += hist[s];
     present += hist[s] > 0;
   }
   int sum = 0;
-  for (int s = 0; s < nsym; ++s) {
+#pragma unroll
+  for (int s = 0; s < 16; ++s) {
     int c = 0;
     if (hist[s]) {
       // weight counts (<= 256) times the table size (<= 64): 32 bits do
       c = int((hist[s] * uint32_t(size) + total / 2) / total);
       c = c < 1 ? 1 : (c > half ? half : c);
     }
-    norm[s] = int16_t(c);
+    norm[s] = c;
     sum += c;
   }
   if (present == 1) { // a second symbol takes the other half
-    for (int s = 0; s < nsym; ++s)
-      if (!hist[s]) {
-        norm[s] = int16_t(size - sum);
+    bool done = false;
+#pragma unroll
+    for (int s = 0; s < 16; ++s)
+      if (!done && s < nsym && !hist[s]) {
+        norm[s] = size - sum;
         sum = size;
-        break;
+        done = true;
       }
   }
   while (sum > size) { // take from the largest
-    int best = -1;
-    for (int s = 0; s < nsym; ++s)
-      if (norm[s] > 1 && (best < 0 || norm[s] > norm[best]))
+    int best = -1, bv = 0;
+#pragma unroll
+    for (int s = 0; s < 16; ++s)
+      if (norm[s] > 1 && (best < 0 || norm[s] > bv)) {
         best = s;
-    norm[best]--;
+        bv = norm[s];
+      }
+#pragma unroll
+    for (int s = 0; s < 16; ++s)
+      if (s == best)
+        norm[s]--;
     --sum;
   }
   while (sum < size) { // give to the most under-represented that has room
     int best = -1;
-    for (int s = 0; s < nsym; ++s)
+    uint32_t bh = 0;
+    int bn = 0;
+#pragma unroll
+    for (int s = 0; s < 16; ++s)
       if (hist[s] && norm[s] < half &&
-          (best < 0 || uint64_t(hist[s]) * uint64_t(norm[best]) >
-                         uint64_t(hist[best]) * uint64_t(norm[s])))
+          (best < 0 || uint64_t(hist[s]) * uint64_t(bn) > uint64_t(bh) * uint64_t(norm[s]))) {
         best = s;
+        bh = hist[s];
+        bn = norm[s];
+      }
     if (best < 0) // everything capped: an absent symbol takes the rest
-      for (int s = 0; s < nsym && best < 0; ++s)
-        if (!hist[s] && norm[s] < half)
+#pragma unroll
+      for (int s = 0; s < 16; ++s)
+        if (best < 0 && s < nsym && !hist[s] && norm[s] < half)
           best = s;
-    norm[best]++;
+#pragma unroll
+    for (int s = 0; s < 16; ++s)
+      if (s == best)
+        norm[s]++;
     ++sum;
   }
+#pragma unroll
+  for (int s = 0; s < 16; ++s)
+    if (s < nsym)
+      norm_s[s] = int16_t(norm[s]);
 }
 
 // FSE table description (RFC 8878 4.1.1), forward bitstream.
@@ -806,9 +835,18 @@ __device__ void huff_describe(TableShared& T, int tid)
   if (tid == 0)
     c.maxw = 0;
   __syncthreads();
-  if (tid < nw) {
-    atomicAdd(&x.whist[w[tid]], 1u);
-    atomicMax(&c.maxw, uint32_t(w[tid]));
+  {
+    // weight histogram and largest weight: one shared atomic per distinct
+    // weight and warp (a few weights shared by many symbols serialise)
+    const uint32_t key = tid < nw ? uint32_t(w[tid]) : ~0u;
+    const unsigned peers = __match_any_sync(0xffffffffu, key);
+    if (tid < nw && lane == __ffs(int(peers)) - 1)
+      atomicAdd(&x.whist[key], uint32_t(__popc(peers)));
+    uint32_t mx = tid < nw ? uint32_t(w[tid]) : 0u;
+    for (int o = 16; o; o >>= 1)
+      mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if (lane == 0 && mx)
+      atomicMax(&c.maxw, mx);
   }
   __syncthreads();
   constexpr int al = 6;
@@ -999,8 +1037,20 @@ zstd_table_k(CodecBatch b,
         }
       }
       T.sorted[rank] = uint16_t(tid);
-      atomicAdd(&T.nsym, 1u);
-      atomicAdd(&T.total, fi);
+    }
+  }
+  {
+    // the used symbols and their total count: warp sums, one shared atomic
+    // per warp (256 on one address serialise)
+    const uint32_t fi = tid < 256 ? T.hist[tid] : 0;
+    uint32_t cnt = fi ? 1u : 0u, tot = fi;
+    for (int o = 16; o; o >>= 1) {
+      cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+      tot += __shfl_xor_sync(0xffffffffu, tot, o);
+    }
+    if (lane == 0 && cnt) {
+      atomicAdd(&T.nsym, cnt);
+      atomicAdd(&T.total, tot);
     }
   }
   __syncthreads();
@@ -1080,10 +1130,14 @@ zstd_table_k(CodecBatch b,
       }
       __syncthreads();
     }
-    // lengths per depth, leaves deeper than kHufMaxBits clamped
-    if (tid < n) {
-      const uint32_t d = dist[tid];
-      atomicAdd(&x.count_w[d > kHufMaxBits ? kHufMaxBits : d], 1u);
+    // lengths per depth, leaves deeper than kHufMaxBits clamped: one
+    // shared atomic per depth and warp
+    {
+      const uint32_t d = tid < n ? uint32_t(dist[tid]) : 0u;
+      const uint32_t key = tid < n ? (d > kHufMaxBits ? kHufMaxBits : d) : ~0u;
+      const unsigned peers = __match_any_sync(0xffffffffu, key);
+      if (tid < n && lane == __ffs(int(peers)) - 1)
+        atomicAdd(&x.count_w[key], uint32_t(__popc(peers)));
     }
     __syncthreads();
     if (tid == 0) {
@@ -1175,8 +1229,14 @@ zstd_table_k(CodecBatch b,
     if (tid == 0)
       h.last = 0;
     __syncthreads();
-    if (sym < 256 && len > 0)
-      atomicMax(&h.last, sym);
+    {
+      // warp maximum first: one shared atomic per warp
+      uint32_t mx = sym < 256 && len > 0 ? uint32_t(sym) : 0u;
+      for (int o = 16; o; o >>= 1)
+        mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+      if (lane == 0 && mx)
+        atomicMax(&h.last, mx);
+    }
     // (h.last is read after the barrier below)
     __syncthreads();
     if (sym < h.last)
