@@ -48,8 +48,7 @@ struct DeviceRes
   uint8_t* out = nullptr;
   size_t out_bytes = 0;
   uint64_t* sizes = nullptr;
-  ChunkRef* refs = nullptr;
-  uint32_t refs_n = 0;
+  ChunkRef* refs = nullptr; // kMaxSample entries
   double d2h_gbs = 0;
 };
 
@@ -202,7 +201,6 @@ bool tune(const TuneKey& key,
     if (cudaMalloc(&R.refs, kMaxSample * sizeof(ChunkRef)) != cudaSuccess ||
         cudaMalloc(&R.sizes, kMaxSample * sizeof(uint64_t)) != cudaSuccess)
       return false;
-    R.refs_n = kMaxSample;
   }
   std::vector<ChunkRef> h(n);
   for (uint32_t i = 0; i < n; ++i)
